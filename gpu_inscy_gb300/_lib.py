@@ -1,0 +1,140 @@
+"""ctypes binding of libinscy_gb300.so (the C ABI declared in include/inscy_gb300.h).
+
+The CUDA library is the product: if it is missing this module raises, there
+is no fallback path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libinscy_gb300.so")
+
+INSCY_OK = 0
+INSCY_ERR_ARG = 1
+INSCY_ERR_CUDA = 2
+INSCY_ERR_UNSUPPORTED = 3
+INSCY_ERR_LIMIT = 4
+INSCY_ERR_INTERNAL = 5
+MODE_PLAIN = 0
+MODE_BATCHED = 1
+
+# every symbol include/inscy_gb300.h declares
+EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_result_count", "inscy_result_n",
+           "inscy_result_subspace", "inscy_result_labels", "inscy_result_stats", "inscy_result_free",
+           "inscy_last_error", "inscy_version"]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("neighborhood_size", ctypes.c_float), ("F", ctypes.c_float), ("num_obj", ctypes.c_int),
+                ("min_size", ctypes.c_int), ("r", ctypes.c_float), ("number_of_cells", ctypes.c_int),
+                ("rectangular", ctypes.c_int), ("entropy_order", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_double) for name in
+                ("ms_total", "ms_setup", "ms_density", "ms_density_pass1", "ms_tree", "ms_cluster", "ms_replay",
+                 "density_bytes", "tree_bytes")] + \
+               [(name, ctypes.c_longlong) for name in
+                ("density_launches_pass1", "kernel_launches", "calls", "regions", "subspaces", "candidates",
+                 "levels", "h2d_bytes", "d2h_bytes")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class InscyError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("inscy error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libinscy_gb300.so not found at %s; build it with "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i64, c_int = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    lib.inscy_run.argtypes = [vp, i64, c_int, ctypes.POINTER(Params), c_int, ctypes.POINTER(vp)]
+    lib.inscy_run_device.argtypes = [vp, i64, c_int, ctypes.POINTER(Params), c_int, vp, ctypes.POINTER(vp)]
+    lib.inscy_run_batch.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(c_int), c_int,
+                                    ctypes.POINTER(Params), c_int, ctypes.POINTER(vp)]
+    lib.inscy_result_count.argtypes = [vp]
+    lib.inscy_result_n.argtypes = [vp]
+    lib.inscy_result_n.restype = i64
+    lib.inscy_result_subspace.argtypes = [vp, c_int, vp, c_int]
+    lib.inscy_result_labels.argtypes = [vp, c_int, vp]
+    lib.inscy_result_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.inscy_result_free.argtypes = [vp]
+    lib.inscy_result_free.restype = None
+    lib.inscy_last_error.restype = ctypes.c_char_p
+    lib.inscy_version.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def make_params(neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectangular=False, entropy_order=0):
+    return Params(float(neighborhood_size), float(F), int(num_obj), int(min_size), float(r), int(number_of_cells),
+                  int(bool(rectangular)), int(entropy_order))
+
+
+def check(rc):
+    if rc != INSCY_OK:
+        raise InscyError(rc, load().inscy_last_error().decode())
+
+
+def collect(handle, free=True):
+    """Turn a result handle into (subspaces: list[list[int]], labels: int32 [k, n], stats)."""
+    lib = load()
+    try:
+        k = lib.inscy_result_count(handle)
+        n = lib.inscy_result_n(handle)
+        dims = np.zeros(64, np.int32)
+        subspaces = []
+        labels = np.empty((k, n), np.int32)
+        for i in range(k):
+            m = lib.inscy_result_subspace(handle, i, dims.ctypes.data, 64)
+            subspaces.append([int(x) for x in dims[:m]])
+            if n:
+                check(lib.inscy_result_labels(handle, i, labels[i].ctypes.data))
+        st = Stats()
+        check(lib.inscy_result_stats(handle, ctypes.byref(st)))
+        return subspaces, labels, st.as_dict()
+    finally:
+        if free:
+            lib.inscy_result_free(handle)
+
+
+def run_host(X, params, mode=MODE_PLAIN):
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    if X.ndim != 2:
+        raise ValueError("X must be [n, d]")
+    h = ctypes.c_void_p()
+    check(load().inscy_run(X.ctypes.data, X.shape[0], X.shape[1], ctypes.byref(params), mode, ctypes.byref(h)))
+    return collect(h)
+
+
+def run_device(ptr, n, d, params, stream=0, mode=MODE_PLAIN):
+    h = ctypes.c_void_p()
+    check(load().inscy_run_device(ctypes.c_void_p(ptr), n, d, ctypes.byref(params), mode, ctypes.c_void_p(stream),
+                                  ctypes.byref(h)))
+    return collect(h)
+
+
+def run_batch(Xs, params, mode=MODE_BATCHED):
+    Xs = [np.ascontiguousarray(x, dtype=np.float32) for x in Xs]
+    B = len(Xs)
+    ptrs = (ctypes.c_void_p * B)(*[x.ctypes.data for x in Xs])
+    ns = (ctypes.c_int64 * B)(*[x.shape[0] for x in Xs])
+    ds = (ctypes.c_int * B)(*[x.shape[1] for x in Xs])
+    outs = (ctypes.c_void_p * B)()
+    check(load().inscy_run_batch(ptrs, ns, ds, B, ctypes.byref(params), mode, outs))
+    return [collect(outs[i]) for i in range(B)]

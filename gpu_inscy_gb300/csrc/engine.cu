@@ -1,0 +1,1199 @@
+// Host engine of the GB300 INSCY path and its C ABI (include/inscy_gb300.h).
+//
+// The reference runs INSCY as a depth-first recursion (INSCYCPU3Weak,
+// InscyNodeCpu.cu:159-235; the GPU forms InscyArrayGpu4/5,
+// InscyArrayGpuMulti2.cu:569-836, keep that recursion on the host and launch
+// small kernels per node).  Here the recursion is split in two:
+//
+//  1. Expansion, level by level over the subspace lattice, on the GPU.
+//     Everything that decides *which* recursion nodes exist -- restrict,
+//     mergeWithNeighbors, the weak-density prune and the min_size test -- is
+//     a pure function of the node, so all nodes of one depth are expanded
+//     together: one density launch for every (subspace, point) of the level,
+//     one restrict/merge/prune launch for every (node, dim), one union-find
+//     for every subspace that has a surviving node.
+//  2. Commit, in the reference's depth-first order, on the host: the
+//     pruneRedundancy gate (ScyTreeNode.cu:669-734), the BFS label
+//     numbering (ClusteringCpu.cu:317-389) and join (util.cu:655-743) read
+//     and write the global result map, so they replay the exact DFS order
+//     over the data the GPU produced.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/inscy_gb300.h"
+#include "inscy_common.cuh"
+#include "inscy_kernels.h"
+#include "inscy_prims.cuh"
+
+namespace inscy {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                            \
+  do {                                                                                                   \
+    cudaError_t e_ = (x);                                                                                \
+    if (e_ != cudaSuccess)                                                                               \
+      throw ::inscy::Error(INSCY_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_) + " (" + __FILE__ + \
+                                      ":" + std::to_string(__LINE__) + ")");                             \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// density thresholds, computed on the host with the reference's formulas and
+// types (ClusteringCpu.cu:27, 36-38, 136-164)
+// ---------------------------------------------------------------------------
+const double kPi = 3.14;  // ClusteringCpu.cu:27
+static float omega_of(int k) { return (float)(2.0 / ((double)k + 2.0)); }
+static float gamma_of(int m) {
+  if (m == 2) return 1.0f;
+  if (m == 1) return (float)std::sqrt(kPi);
+  return (float)(((double)m / 2.0 - 1.0) * (double)gamma_of(m - 2));
+}
+static float cball_of(int k) {
+  float r = (float)std::pow(kPi, (double)k / 2.0);
+  return r / gamma_of(k + 2);
+}
+static float alpha_of(int k, float eps, int n) {
+  float r = (float)((double)(2 * n) * std::pow((double)eps, (double)k) * (double)cball_of(k));
+  r = (float)((double)r / (std::pow(1.0, (double)k) * (double)(k + 2)));
+  return r;
+}
+static float expden_of(int k, float eps, int n) {
+  float r = (float)((double)((float)n * cball_of(k)) * std::pow((double)eps, (double)k));
+  r = (float)((double)r / std::pow(1.0, (double)k));
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// result map ordering (vec_cmp, util.cu:633-653): compare from the last dim
+// ---------------------------------------------------------------------------
+struct SubspaceOrder {
+  bool operator()(const std::vector<int>& a, const std::vector<int>& b) const {
+    int i = (int)a.size() - 1, j = (int)b.size() - 1;
+    while (a[i] == b[j]) {
+      --i;
+      --j;
+      if (i < 0 || j < 0) return i < j;
+    }
+    return a[i] < b[j];
+  }
+};
+
+static std::vector<int> dims_of(uint64_t m) {
+  std::vector<int> v;
+  for (int k = 0; k < 64; ++k)
+    if ((m >> k) & 1ull) v.push_back(k);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// device memory: stream-ordered allocations from a retained pool (no
+// cudaMalloc on the hot path once the pool has grown)
+// ---------------------------------------------------------------------------
+class Pool {
+ public:
+  explicit Pool(int device) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    CK(cudaMemPoolCreate(&pool_, &props));
+    uint64_t thr = UINT64_MAX;
+    CK(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &thr));
+  }
+  ~Pool() { cudaMemPoolDestroy(pool_); }
+  void* get(size_t bytes, cudaStream_t s) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    CK(cudaMallocFromPoolAsync(&p, bytes, pool_, s));
+    return p;
+  }
+  void put(void* p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+  }
+
+ private:
+  cudaMemPool_t pool_;
+};
+
+// a set of allocations released together
+class Scope {
+ public:
+  Scope(Pool& p, cudaStream_t s) : pool_(p), s_(s) {}
+  ~Scope() { release(); }
+  template <class T>
+  T* get(size_t count) {
+    void* p = pool_.get(count * sizeof(T), s_);
+    ptrs_.push_back(p);
+    return (T*)p;
+  }
+  void release() {
+    for (void* p : ptrs_) pool_.put(p, s_);
+    ptrs_.clear();
+  }
+  void adopt(Scope& o) {
+    ptrs_.insert(ptrs_.end(), o.ptrs_.begin(), o.ptrs_.end());
+    o.ptrs_.clear();
+  }
+
+ private:
+  Pool& pool_;
+  cudaStream_t s_;
+  std::vector<void*> ptrs_;
+};
+
+// pinned staging for device-to-host copies
+class Pinned {
+ public:
+  ~Pinned() {
+    if (p_) cudaFreeHost(p_);
+  }
+  void* get(size_t bytes) {
+    if (bytes > cap_) {
+      if (p_) cudaFreeHost(p_);
+      p_ = nullptr;
+      cap_ = std::max(bytes, cap_ * 2);
+      CK(cudaMallocHost(&p_, cap_));
+    }
+    return p_;
+  }
+
+ private:
+  void* p_ = nullptr;
+  size_t cap_ = 0;
+};
+
+// ---------------------------------------------------------------------------
+// host-side record of the recursion (for the ordered commit)
+// ---------------------------------------------------------------------------
+struct HRegion {
+  int dim;
+  int passed;
+  int child;  // index into calls_ (passed only)
+};
+
+struct HCall {
+  uint64_t rmask = 0;
+  int f = 0;
+  int level = 0;
+  int npts = 0;
+  long long pts_off = 0;  // into levels_[level].pts (its leaf order)
+  int norder = 0;         // components in first-seed order, at levels_[level].order[pts_off ...]
+  int csub = -1;          // clustered subspace (its own subspace) in subs_
+  std::vector<HRegion> regions;  // ordered by (dim, cell run)
+};
+
+struct HLevel {
+  std::vector<int> pts;
+  std::vector<int> order;
+};
+
+struct HSub {  // components of one clustered subspace
+  std::vector<long long> moff;
+  std::vector<int> members;
+  std::vector<long long> boff;
+  std::vector<int> borders;
+};
+
+struct Entry {
+  uint64_t mask = 0;
+  std::vector<int> lab;
+  int maxv = 0;
+  std::vector<int> szp;  // size of the point's cluster (0: none)
+};
+
+struct HostParams {
+  float eps, F, r;
+  int num_obj, min_size, cells, rect;
+};
+
+// ---------------------------------------------------------------------------
+// the engine (one run at a time; device resources are kept between runs)
+// ---------------------------------------------------------------------------
+class Engine {
+ public:
+  Engine() {
+    CK(cudaGetDevice(&device_));
+    pool_.reset(new Pool(device_));
+    CK(cudaEventCreate(&ev0_));
+    CK(cudaEventCreate(&ev1_));
+  }
+  ~Engine() {
+    cudaEventDestroy(ev0_);
+    cudaEventDestroy(ev1_);
+  }
+
+  void run(const float* X, bool on_device, long long n, int d, const HostParams& hp, cudaStream_t s,
+           std::vector<std::vector<int>>& out_dims, std::vector<std::vector<int>>& out_labels, inscy_stats& st);
+
+ private:
+  // timing helper: device time of the work queued by f()
+  template <class Fn>
+  double timed(cudaStream_t s, Fn f) {
+    CK(cudaEventRecord(ev0_, s));
+    f();
+    CK(cudaEventRecord(ev1_, s));
+    CK(cudaEventSynchronize(ev1_));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    return ms;
+  }
+  void d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (!bytes) return;
+    void* st = pinned_.get(bytes);
+    CK(cudaMemcpyAsync(st, src, bytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::memcpy(dst, st, bytes);
+    stats_.d2h_bytes += (long long)bytes;
+  }
+  void h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (!bytes) return;
+    void* st = pinned_.get(bytes);
+    std::memcpy(st, src, bytes);
+    CK(cudaMemcpyAsync(dst, st, bytes, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    stats_.h2d_bytes += (long long)bytes;
+  }
+  template <class T>
+  T scalar(const T* dev, cudaStream_t s) {
+    T v;
+    d2h(&v, dev, sizeof(T), s);
+    return v;
+  }
+  void* scan_sums(long long n, cudaStream_t s, Scope& sc) {
+    long long nt = (n + 2047) / 2048 + 1;
+    return sc.get<long long>((size_t)nt);
+  }
+
+  // commit
+  void replay(int ci);
+  bool prune_redundancy(const HCall& c, uint64_t smask);
+  void cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>& touched, int& nlabels);
+  void join(std::vector<int>& V, std::vector<int>& touched, int nlabels, uint64_t smask);
+
+  int device_ = 0;
+  std::unique_ptr<Pool> pool_;
+  Pinned pinned_;
+  cudaEvent_t ev0_, ev1_;
+
+  // per run
+  HostParams hp_;
+  long long n_ = 0;
+  int d_ = 0;
+  std::vector<HCall> calls_;
+  std::vector<HLevel> levels_;
+  std::vector<HSub> subs_;
+  std::map<std::vector<int>, Entry, SubspaceOrder> result_;
+  std::vector<std::vector<int>> vbuf_;  // one n-vector of labels per recursion depth
+  inscy_stats stats_;
+};
+
+// ---------------------------------------------------------------------------
+void Engine::run(const float* X, bool on_device, long long n, int d, const HostParams& hp, cudaStream_t s,
+                 std::vector<std::vector<int>>& out_dims, std::vector<std::vector<int>>& out_labels, inscy_stats& st) {
+  auto t_start = std::chrono::steady_clock::now();
+  std::memset(&stats_, 0, sizeof(stats_));
+  hp_ = hp;
+  n_ = n;
+  d_ = d;
+  calls_.clear();
+  levels_.clear();
+  subs_.clear();
+  result_.clear();
+  out_dims.clear();
+  out_labels.clear();
+  if (n == 0) {
+    st = stats_;
+    return;
+  }
+  const int ni = (int)n;
+  const int cells = hp.cells;
+  const int G = (int)std::ceil(1.0 / (double)hp.eps);  // inscy_map.cpp:243
+  if (G > 256) throw Error(INSCY_ERR_LIMIT, "ceil(1/neighborhood_size) = " + std::to_string(G) + " > 256");
+  const float csz = 1.0f / (float)cells;
+  const float fsz = 1.0f / (float)G;
+  const int W = (ni + 31) / 32;
+  long long launches = 0;
+
+  // thresholds: weak density uses all d dims (ScyTreeNode.cu:604-606), the
+  // clustering density |S| (ClusteringCpu.cu:166-183).  A point that can be
+  // dense in some descendant subspace has phi >= thr_keep at every prefix.
+  std::vector<float> thr_dense(d + 2, 0.f), thr_keep(d + 2, 0.f);
+  float thr_weak;
+  if (hp.rect) {
+    thr_weak = std::max(hp.F * expden_of(d, hp.eps, ni), (float)hp.num_obj);
+    for (int k = 1; k <= d; ++k) thr_dense[k] = std::max(hp.F * expden_of(k, hp.eps, ni), (float)hp.num_obj);
+  } else {
+    thr_weak = std::max(hp.F * alpha_of(d, hp.eps, ni), (float)hp.num_obj * omega_of(d));
+    for (int k = 1; k <= d; ++k)
+      thr_dense[k] = std::max(hp.F * alpha_of(k, hp.eps, ni), (float)hp.num_obj * omega_of(k));
+  }
+  for (int k = 1; k <= d; ++k) {
+    float t = thr_weak;
+    for (int j = k; j <= d; ++j) t = std::min(t, thr_dense[j]);
+    thr_keep[k] = t;
+  }
+
+  Scope persist(*pool_, s);
+  // ------------------------------------------------------------------ setup
+  auto t_setup0 = std::chrono::steady_clock::now();
+  const float* dX = X;
+  if (!on_device) {
+    float* x = persist.get<float>((size_t)n * d);
+    void* stg = pinned_.get((size_t)n * d * sizeof(float));
+    std::memcpy(stg, X, (size_t)n * d * sizeof(float));
+    CK(cudaMemcpyAsync(x, stg, (size_t)n * d * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the staging buffer is reused below
+    stats_.h2d_bytes += (long long)n * d * sizeof(float);
+    dX = x;
+  } else {
+    // device input: every value must be a number in [0, 1] (cell indices
+    // index the per-dim buckets)
+    int* bad = persist.get<int>(1);
+    CK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+    launch_check_range(dX, (long long)n * d, bad, s);
+    if (scalar(bad, s)) throw Error(INSCY_ERR_ARG, "X has a value outside [0, 1]");
+  }
+  uint8_t* dcc = persist.get<uint8_t>((size_t)n * d);
+  uint8_t* dfc = persist.get<uint8_t>((size_t)n * d);
+  unsigned long long* dgz = persist.get<unsigned long long>((size_t)n);
+  float* dthr = persist.get<float>(2 * (d + 2));
+  h2d(dthr, thr_dense.data(), sizeof(float) * (d + 2), s);
+  h2d(dthr + d + 2, thr_keep.data(), sizeof(float) * (d + 2), s);
+  launch_prep(dX, ni, d, cells, csz, G, fsz, hp.eps, dcc, dfc, dgz, s);
+  ++launches;
+  int* drank = persist.get<int>(n);
+  int* dbucket = persist.get<int>((size_t)n * d);
+  int* dboff = persist.get<int>((size_t)d * (G + 1));
+  long long* dcoff = persist.get<long long>((size_t)d * G + 1);
+  int* dcand = nullptr;
+  int* droot = nullptr;
+  {
+    Scope tmp(*pool_, s);
+    int nb = (ni + kSortTile - 1) / kSortTile;
+    int* hist = tmp.get<int>((size_t)256 * nb);
+    int* htot = tmp.get<int>(1);
+    int* starts = tmp.get<int>(257);
+    void* sums = scan_sums(256LL * nb, s, tmp);
+    int* a = tmp.get<int>(n);
+    int* b = tmp.get<int>(n);
+    // neighbourhood-trie leaf order: lexicographic fine cells, dims in
+    // level order, ties by id -> LSD passes from the last dim
+    launch_iota(a, ni, s);
+    ++launches;
+    for (int k = d - 1; k >= 0; --k) {
+      launch_byte_sort_pass(a, b, ni, dfc, d, k, hist, htot, nullptr, sums, s);
+      launches += 5;
+      std::swap(a, b);
+    }
+    launch_scatter_rank(a, ni, drank, s);
+    ++launches;
+    // per-dim cell buckets, each in trie order
+    for (int k = 0; k < d; ++k) {
+      launch_byte_sort_pass(a, dbucket + (size_t)k * n, ni, dfc, d, k, hist, htot, starts, sums, s);
+      launches += 6;
+      CK(cudaMemcpyAsync(dboff + (size_t)k * (G + 1), starts, sizeof(int) * (G + 1), cudaMemcpyDeviceToDevice, s));
+    }
+    std::vector<int> hboff((size_t)d * (G + 1));
+    d2h(hboff.data(), dboff, hboff.size() * sizeof(int), s);
+    std::vector<long long> hcoff((size_t)d * G + 1);
+    long long tot = 0;
+    for (int k = 0; k < d; ++k)
+      for (int c = 0; c < G; ++c) {
+        hcoff[(size_t)k * G + c] = tot;
+        const int* bo = hboff.data() + (size_t)k * (G + 1);
+        for (int b2 = c - 1; b2 <= c + 1; ++b2)
+          if (b2 >= 0 && b2 < G) tot += bo[b2 + 1] - bo[b2];
+      }
+    hcoff[(size_t)d * G] = tot;
+    h2d(dcoff, hcoff.data(), hcoff.size() * sizeof(long long), s);
+    dcand = persist.get<int>((size_t)tot);
+    launch_candidate_lists(ni, d, G, dbucket, dboff, drank, dfc, dcoff, dcand, s);
+    ++launches;
+    // root SCY-tree leaf order: coarse cells in dim order, ties by id
+    launch_iota(a, ni, s);
+    ++launches;
+    for (int k = d - 1; k >= 0; --k) {
+      launch_byte_sort_pass(a, b, ni, dcc, d, k, hist, htot, nullptr, sums, s);
+      launches += 5;
+      std::swap(a, b);
+    }
+    droot = persist.get<int>(n);
+    CK(cudaMemcpyAsync(droot, a, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  stats_.ms_setup = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup0).count();
+
+  // ------------------------------------------------------------ expansion
+  // current calls (device descriptors + host records)
+  std::vector<CallDesc> hcalls(1);
+  hcalls[0].pts_off = 0;
+  hcalls[0].ghost_off = 0;
+  hcalls[0].rmask = 0;
+  hcalls[0].npts = ni;
+  hcalls[0].f = 0;
+  hcalls[0].nghost = 0;
+  hcalls[0].sub = -1;
+  hcalls[0].child_sub = 0;
+  hcalls[0].nrestricted = 0;
+  std::vector<int> call_ids(1, 0);
+  calls_.push_back(HCall());
+  calls_[0].npts = ni;
+  levels_.push_back(HLevel());
+
+  std::unique_ptr<Scope> cur_pts(new Scope(*pool_, s));  // the current calls' points and ghosts
+  int* d_pts = droot;
+  int2* d_ghosts = cur_pts->get<int2>(1);
+
+  struct PrevLevel {
+    std::unique_ptr<Scope> mem;
+    std::vector<SubDesc> subs;
+    std::vector<long long> kstart;  // nsubs + 1
+    int* keep_ids = nullptr;
+    long long* keep_loff = nullptr;
+    int* keep_lcnt = nullptr;
+    int* lids = nullptr;
+    float* lacc = nullptr;
+  } prev;
+
+  int level = 0;
+  while (!hcalls.empty()) {
+    ++level;
+    stats_.levels = level;
+    Scope lv(*pool_, s);  // this level's temporaries
+    std::unique_ptr<Scope> keepmem(new Scope(*pool_, s));  // this level's kept lists (live one more level)
+
+    // ---- 1. subspaces of this level: children of the calls' subspaces
+    std::vector<SubDesc> subs;
+    std::map<int, int> child_base;  // parent subspace -> first child
+    for (auto& c : hcalls) {
+      auto it = child_base.find(c.sub);
+      if (it == child_base.end()) {
+        int base = (int)subs.size();
+        child_base[c.sub] = base;
+        uint64_t pm = c.rmask;
+        int first = c.f;
+        long long nq = c.sub < 0 ? n : prev.kstart[c.sub + 1] - prev.kstart[c.sub];
+        long long qo = c.sub < 0 ? 0 : prev.kstart[c.sub];
+        for (int D = first; D < d; ++D) {
+          SubDesc S;
+          S.mask = pm | (1ull << D);
+          S.dim = D;
+          S.nsub = __builtin_popcountll(S.mask);
+          S.parent = c.sub;
+          S.nquery = (int)nq;
+          S.item_off = 0;
+          S.query_off = qo;
+          S.plist_base = 0;
+          S.bitmap_off = 0;
+          subs.push_back(S);
+        }
+        c.child_sub = base;
+      } else {
+        c.child_sub = it->second;
+      }
+    }
+    const int nsubs = (int)subs.size();
+    long long nitems = 0;
+    for (int i = 0; i < nsubs; ++i) {
+      subs[i].item_off = nitems;
+      subs[i].bitmap_off = (long long)i * 3 * W;
+      nitems += subs[i].nquery;
+    }
+    stats_.subspaces += nsubs;
+    SubDesc* dsubs = lv.get<SubDesc>(nsubs);
+    h2d(dsubs, subs.data(), sizeof(SubDesc) * nsubs, s);
+
+    // ---- 2. density pass 1
+    int* dcnt = lv.get<int>(nitems);
+    uint8_t* dflags = lv.get<uint8_t>(nitems);
+    unsigned* dbm = keepmem->get<unsigned>((size_t)nsubs * 3 * W);
+    CK(cudaMemsetAsync(dbm, 0, sizeof(unsigned) * (size_t)nsubs * 3 * W, s));
+    DensityLaunch DL;
+    std::memset(&DL, 0, sizeof(DL));
+    DL.subs = dsubs;
+    DL.nsubs = nsubs;
+    DL.nitems = nitems;
+    DL.X = dX;
+    DL.fc = dfc;
+    DL.n = ni;
+    DL.d = d;
+    DL.G = G;
+    DL.eps = hp.eps;
+    DL.rect = hp.rect;
+    DL.thr_weak = thr_weak;
+    DL.thr_dense = dthr;
+    DL.thr_keep = dthr + d + 2;
+    DL.cand_off = dcoff;
+    DL.cand_pts = dcand;
+    DL.prev_keep = prev.keep_ids;
+    DL.prev_loff = prev.keep_loff;
+    DL.prev_lcnt = prev.keep_lcnt;
+    DL.prev_lids = prev.lids;
+    DL.prev_lacc = prev.lacc;
+    DL.cnt = dcnt;
+    DL.flags = dflags;
+    DL.bitmaps = dbm;
+    DL.words = W;
+    double ms1 = timed(s, [&] { launch_density(DL, false, s); });
+    stats_.ms_density += ms1;
+    stats_.ms_density_pass1 += ms1;
+    stats_.density_launches_pass1 += 1;
+    ++launches;
+
+    // ---- 3. kept items: list offsets and kept-point arrays
+    int* dkcnt = lv.get<int>(nitems);
+    int* dkflag = lv.get<int>(nitems);
+    long long* dloff = lv.get<long long>(nitems);
+    long long* dkpos = lv.get<long long>(nitems + 1);
+    long long* dtot = lv.get<long long>(2);
+    void* sums = scan_sums(std::max(nitems, (long long)nsubs * W) + 1, s, lv);
+    launch_keep_counts(dcnt, dflags, nitems, dkcnt, dkflag, s);
+    launch_exclusive_scan_i2ll(dkcnt, dloff, nitems, dtot, sums, s);
+    launch_exclusive_scan_i2ll(dkflag, dkpos, nitems, dtot + 1, sums, s);
+    launches += 7;
+    long long htot[2];
+    d2h(htot, dtot, sizeof(htot), s);
+    const long long L = htot[0], K = htot[1];
+    int* keep_ids = keepmem->get<int>(K);
+    long long* keep_loff = keepmem->get<long long>(K);
+    int* keep_lcnt = keepmem->get<int>(K);
+    int* lids = keepmem->get<int>(L);
+    float* lacc = keepmem->get<float>(L);
+    DL.out_off = dloff;
+    DL.out_ids = lids;
+    DL.out_acc = lacc;
+    stats_.ms_density += timed(s, [&] { launch_density(DL, true, s); });
+    launch_keep_compact(dsubs, nsubs, nitems, dflags, dcnt, dkpos, dloff, prev.keep_ids, keep_ids, keep_loff,
+                        keep_lcnt, s);
+    launches += 2;
+    // kept-index start of every subspace
+    long long* dkstart = keepmem->get<long long>(nsubs + 1);
+    launch_gather_kstart(dsubs, nsubs, dkpos, nitems, K, dkstart, s);
+    ++launches;
+    std::vector<long long> kstart(nsubs + 1);
+    d2h(kstart.data(), dkstart, sizeof(long long) * (nsubs + 1), s);
+    // global rank of every kept bit: prefix of the kept-bitmap popcounts
+    int* dkwr = keepmem->get<int>((size_t)nsubs * W + 1);
+    {
+      int* pc = lv.get<int>((size_t)nsubs * W + 1);
+      for (int i = 0; i < nsubs; ++i) {
+        launch_word_popc(dbm + (size_t)i * 3 * W + 2 * W, W, pc + (size_t)i * W, s);
+        ++launches;
+      }
+      int* dt = lv.get<int>(1);
+      launch_exclusive_scan_int(pc, dkwr, (long long)nsubs * W, dt, sums, s);
+      launches += 3;
+    }
+
+    // ---- 4. restrict / merge / prune of every (call, dim)
+    const int ncalls = (int)hcalls.size();
+    std::vector<long long> work_off(ncalls), work_scr;
+    long long nwork = 0, scr = 0, pts_cap = 0, ghost_in = 0;
+    for (int i = 0; i < ncalls; ++i) {
+      work_off[i] = nwork;
+      int nd = d - hcalls[i].f;
+      for (int t = 0; t < nd; ++t) {
+        work_scr.push_back(scr);
+        scr += 3LL * hcalls[i].npts + 1;
+      }
+      nwork += nd;
+      pts_cap += (long long)hcalls[i].npts * nd;
+      ghost_in += (long long)hcalls[i].nghost * nd;
+    }
+    stats_.regions += 0;
+    CallDesc* dcalls = lv.get<CallDesc>(ncalls);
+    h2d(dcalls, hcalls.data(), sizeof(CallDesc) * ncalls, s);
+    long long* dwork = lv.get<long long>(ncalls);
+    h2d(dwork, work_off.data(), sizeof(long long) * ncalls, s);
+    long long* dwscr = lv.get<long long>(nwork);
+    h2d(dwscr, work_scr.data(), sizeof(long long) * nwork, s);
+    int* dscr = lv.get<int>(scr);
+    RegionRec* drecs = lv.get<RegionRec>((size_t)nwork * cells);
+    int* dnrecs = lv.get<int>(nwork);
+    std::unique_ptr<Scope> next_pts(new Scope(*pool_, s));
+    int* dout_pts = next_pts->get<int>(pts_cap);
+    unsigned long long* dtops = lv.get<unsigned long long>(2);
+    int* derr = lv.get<int>(1);
+    long long ghost_cap = std::max(1024LL, ghost_in + pts_cap / 4);
+    int2* dout_gh = nullptr;
+    std::vector<RegionRec> recs;
+    std::vector<int> nrecs(nwork);
+    unsigned long long tops[2];
+    for (int attempt = 0;; ++attempt) {
+      dout_gh = next_pts->get<int2>(ghost_cap);
+      CK(cudaMemsetAsync(dtops, 0, sizeof(unsigned long long) * 2, s));
+      CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
+      TreeLaunch TL;
+      TL.calls = dcalls;
+      TL.ncalls = ncalls;
+      TL.work_off = dwork;
+      TL.nwork = (int)nwork;
+      TL.pts_in = d_pts;
+      TL.ghosts_in = d_ghosts;
+      TL.cc = dcc;
+      TL.gz = dgz;
+      TL.n = ni;
+      TL.d = d;
+      TL.cells = cells;
+      TL.min_size = hp.min_size;
+      TL.subs = dsubs;
+      TL.bitmaps = dbm;
+      TL.scratch = dscr;
+      TL.work_scratch = dwscr;
+      TL.recs = drecs;
+      TL.nrecs = dnrecs;
+      TL.out_pts = dout_pts;
+      TL.out_pts_top = dtops;
+      TL.out_pts_cap = pts_cap;
+      TL.out_ghosts = dout_gh;
+      TL.out_ghost_top = dtops + 1;
+      TL.out_ghost_cap = ghost_cap;
+      TL.err = derr;
+      stats_.ms_tree += timed(s, [&] { launch_tree_level(TL, s); });
+      ++launches;
+      int err = scalar(derr, s);
+      d2h(tops, dtops, sizeof(tops), s);
+      if (err == 2 && attempt < 4) {
+        ghost_cap = (long long)tops[1] + 1024;
+        continue;
+      }
+      if (err) throw Error(INSCY_ERR_INTERNAL, "level kernel reported error " + std::to_string(err));
+      break;
+    }
+    recs.resize((size_t)nwork * cells);
+    d2h(recs.data(), drecs, sizeof(RegionRec) * recs.size(), s);
+    d2h(nrecs.data(), dnrecs, sizeof(int) * nwork, s);
+    stats_.tree_bytes += 0;
+
+    // ---- 5. next level's calls (host records in the reference's order)
+    std::vector<CallDesc> ncall;
+    std::vector<int> ncall_ids;
+    for (int i = 0; i < ncalls; ++i) {
+      HCall& parent = calls_[call_ids[i]];
+      int nd = d - hcalls[i].f;
+      for (int t = 0; t < nd; ++t) {
+        long long w = work_off[i] + t;
+        for (int r = 0; r < nrecs[w]; ++r) {
+          const RegionRec& R = recs[(size_t)w * cells + r];
+          stats_.regions++;
+          HRegion hr;
+          hr.dim = R.dim;
+          hr.passed = R.passed;
+          hr.child = -1;
+          if (R.passed) {
+            CallDesc c;
+            c.pts_off = R.pts_off;
+            c.ghost_off = R.ghost_off;
+            c.rmask = hcalls[i].rmask | (1ull << R.dim);
+            c.npts = R.npts;
+            c.f = R.dim + 1;
+            c.nghost = R.nghost;
+            c.sub = hcalls[i].child_sub + (R.dim - hcalls[i].f);
+            c.child_sub = 0;
+            c.nrestricted = hcalls[i].nrestricted + 1;
+            ncall.push_back(c);
+            HCall hc;
+            hc.rmask = c.rmask;
+            hc.f = c.f;
+            hc.level = level;
+            hc.npts = c.npts;
+            hc.pts_off = c.pts_off;
+            hr.child = (int)calls_.size();
+            ncall_ids.push_back(hr.child);
+            calls_.push_back(hc);
+          }
+          calls_[call_ids[i]].regions.push_back(hr);
+          (void)parent;
+        }
+      }
+    }
+    stats_.calls += (long long)ncall.size();
+
+    // ---- 6. clustering of the subspaces that gained calls
+    levels_.push_back(HLevel());
+    HLevel& hl = levels_.back();
+    if (!ncall.empty()) {
+      hl.pts.resize(tops[0]);
+      d2h(hl.pts.data(), dout_pts, sizeof(int) * tops[0], s);
+      hl.order.assign(tops[0], 0);
+      std::vector<uint8_t> clustered(nsubs, 0);
+      std::vector<std::vector<int>> sub_calls(nsubs);
+      for (size_t j = 0; j < ncall.size(); ++j) {
+        clustered[ncall[j].sub] = 1;
+        sub_calls[ncall[j].sub].push_back((int)j);
+      }
+      std::vector<int> clist, cslot(nsubs, -1), sc_off(1, 0), sc_list;
+      for (int i = 0; i < nsubs; ++i)
+        if (clustered[i]) {
+          cslot[i] = (int)clist.size();
+          clist.push_back(i);
+          for (int j : sub_calls[i]) sc_list.push_back(j);
+          sc_off.push_back((int)sc_list.size());
+        }
+      const int ncl = (int)clist.size();
+      uint8_t* dcl = lv.get<uint8_t>(nsubs);
+      h2d(dcl, clustered.data(), nsubs, s);
+      int* dclist = lv.get<int>(ncl);
+      h2d(dclist, clist.data(), sizeof(int) * ncl, s);
+      int* dcslot = lv.get<int>(nsubs);
+      h2d(dcslot, cslot.data(), sizeof(int) * nsubs, s);
+      int* dscoff = lv.get<int>(sc_off.size());
+      h2d(dscoff, sc_off.data(), sizeof(int) * sc_off.size(), s);
+      int* dsclist = lv.get<int>(sc_list.size());
+      h2d(dsclist, sc_list.data(), sizeof(int) * sc_list.size(), s);
+      CallDesc* dncall = lv.get<CallDesc>(ncall.size());
+      h2d(dncall, ncall.data(), sizeof(CallDesc) * ncall.size(), s);
+
+      ClusterArgs CA;
+      CA.nsubs = nsubs;
+      CA.subs = dsubs;
+      CA.kstart = dkstart;
+      CA.keep_ids = keep_ids;
+      CA.keep_loff = keep_loff;
+      CA.keep_lcnt = keep_lcnt;
+      CA.lids = lids;
+      CA.bitmaps = dbm;
+      CA.words = W;
+      CA.keep_word_rank = dkwr;
+      CA.clustered = dcl;
+      CA.clustered_list = dclist;
+      CA.nkeep = K;
+      CA.n = ni;
+      CA.uf = lv.get<int>(K + 1);
+      CA.err = derr;
+      CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
+      int* is_root = lv.get<int>(K + 1);
+      int* root_id = lv.get<int>(K + 1);
+      int* comp = lv.get<int>(K + 1);
+      int* dnc = lv.get<int>(1);
+      long long ncomp = 0;
+      std::vector<int> cbase(nsubs + 1);
+      stats_.ms_cluster += timed(s, [&] {
+        launch_uf_init(CA.uf, K, s);
+        launch_uf_union(CA, s);
+        launch_uf_flatten(CA, is_root, s);
+        launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
+      });
+      launches += 6;
+      ncomp = scalar(dnc, s);
+      int* dcbase = lv.get<int>(nsubs + 1);
+      launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);
+      ++launches;
+      d2h(cbase.data(), dcbase, sizeof(int) * (nsubs + 1), s);
+      int* mcount = lv.get<int>(ncomp + 1);
+      int* mfill = lv.get<int>(ncomp + 1);
+      long long* moff = lv.get<long long>(ncomp + 1);
+      int* bcount = lv.get<int>(ncomp + 1);
+      int* bfill = lv.get<int>(ncomp + 1);
+      long long* boff = lv.get<long long>(ncomp + 1);
+      CK(cudaMemsetAsync(mcount, 0, sizeof(int) * (ncomp + 1), s));
+      CK(cudaMemsetAsync(mfill, 0, sizeof(int) * (ncomp + 1), s));
+      CK(cudaMemsetAsync(bcount, 0, sizeof(int) * (ncomp + 1), s));
+      CK(cudaMemsetAsync(bfill, 0, sizeof(int) * (ncomp + 1), s));
+      long long nslots2 = (long long)ncl * n * 2;
+      int* slots = lv.get<int>(nslots2);
+      CK(cudaMemsetAsync(slots, 0xff, sizeof(int) * nslots2, s));
+      const int ovf_cap = 1 << 20;
+      int2* ovf = lv.get<int2>(ovf_cap);
+      int* novf = lv.get<int>(1);
+      CK(cudaMemsetAsync(novf, 0, sizeof(int), s));
+      long long* dmtot = lv.get<long long>(2);
+      stats_.ms_cluster += timed(s, [&] {
+        launch_comp_ids(CA, root_id, comp, mcount, s);
+        launch_exclusive_scan_i2ll(mcount, moff, ncomp, dmtot, sums, s);
+      });
+      launches += 4;
+      long long hm[2];
+      d2h(hm, dmtot, sizeof(long long), s);
+      int* members = lv.get<int>(hm[0] + 1);
+      launch_members(CA, comp, moff, mfill, members, s);
+      launches += 1;
+      int hovf = 0;
+      stats_.ms_cluster += timed(s, [&] { launch_borders(CA, comp, dcslot, slots, ovf, novf, ovf_cap, s); });
+      launches += 1;
+      hovf = scalar(novf, s);
+      if (scalar(derr, s)) throw Error(INSCY_ERR_INTERNAL, "clustering kernels reported an error");
+      hovf = std::min(hovf, ovf_cap);
+      launch_border_count(slots, nslots2, ovf, hovf, bcount, s);
+      launch_exclusive_scan_i2ll(bcount, boff, ncomp, dmtot + 1, sums, s);
+      launches += 5;
+      long long hb;
+      d2h(&hb, dmtot + 1, sizeof(long long), s);
+      int* borders = lv.get<int>(hb + 1);
+      launch_border_fill(slots, nslots2, ni, ovf, hovf, boff, bfill, borders, s);
+      // components of each region in first-seed order
+      int* firstpos = lv.get<int>(ncomp + 1);
+      CK(cudaMemsetAsync(firstpos, 0x7f, sizeof(int) * (ncomp + 1), s));
+      int* order = lv.get<int>(tops[0] + 1);
+      int* order_cnt = lv.get<int>(ncall.size());
+      stats_.ms_cluster += timed(s, [&] {
+        launch_region_order(CA, ncl, comp, dcbase, dscoff, dsclist, dncall, dout_pts, firstpos, order, order_cnt, s);
+      });
+      launches += 3;
+      // to the host
+      std::vector<long long> hmoff(ncomp + 1), hboff(ncomp + 1);
+      d2h(hmoff.data(), moff, sizeof(long long) * ncomp, s);
+      hmoff[ncomp] = hm[0];
+      d2h(hboff.data(), boff, sizeof(long long) * ncomp, s);
+      hboff[ncomp] = hb;
+      std::vector<int> hmem(hm[0]), hbor(hb);
+      d2h(hmem.data(), members, sizeof(int) * hm[0], s);
+      d2h(hbor.data(), borders, sizeof(int) * hb, s);
+      d2h(hl.order.data(), order, sizeof(int) * tops[0], s);
+      std::vector<int> hocnt(ncall.size());
+      d2h(hocnt.data(), order_cnt, sizeof(int) * ncall.size(), s);
+      // one HSub per clustered subspace (component-local offsets)
+      std::vector<int> csub_of(nsubs, -1);
+      for (int i : clist) {
+        HSub hs;
+        long long c0 = cbase[i], c1 = cbase[i + 1];
+        hs.moff.resize(c1 - c0 + 1);
+        hs.boff.resize(c1 - c0 + 1);
+        for (long long c = c0; c <= c1; ++c) {
+          hs.moff[c - c0] = hmoff[c] - hmoff[c0];
+          hs.boff[c - c0] = hboff[c] - hboff[c0];
+        }
+        hs.members.assign(hmem.begin() + hmoff[c0], hmem.begin() + hmoff[c1]);
+        hs.borders.assign(hbor.begin() + hboff[c0], hbor.begin() + hboff[c1]);
+        csub_of[i] = (int)subs_.size();
+        subs_.push_back(std::move(hs));
+      }
+      for (size_t j = 0; j < ncall.size(); ++j) {
+        HCall& hc = calls_[ncall_ids[j]];
+        hc.csub = csub_of[ncall[j].sub];
+        hc.norder = hocnt[j];
+      }
+    }
+
+    // ---- 7. advance: this level's lists become the parent lists
+    prev.mem = std::move(keepmem);
+    prev.subs = subs;
+    prev.kstart = kstart;
+    prev.keep_ids = keep_ids;
+    prev.keep_loff = keep_loff;
+    prev.keep_lcnt = keep_lcnt;
+    prev.lids = lids;
+    prev.lacc = lacc;
+    cur_pts = std::move(next_pts);
+    d_pts = dout_pts;
+    d_ghosts = dout_gh;
+    hcalls.swap(ncall);
+    call_ids.swap(ncall_ids);
+    lv.release();
+    stats_.kernel_launches = launches;
+  }
+  prev.mem.reset();
+  cur_pts.reset();
+  persist.release();
+  CK(cudaStreamSynchronize(s));
+
+  // ---------------------------------------------------------------- commit
+  auto t_rep0 = std::chrono::steady_clock::now();
+  vbuf_.assign(d + 2, std::vector<int>());
+  replay(0);
+  stats_.ms_replay = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_rep0).count();
+  for (auto& e : result_) {
+    out_dims.push_back(e.first);
+    out_labels.push_back(std::move(e.second.lab));
+  }
+  result_.clear();
+  stats_.kernel_launches = launches;
+  stats_.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  st = stats_;
+}
+
+// ---------------------------------------------------------------------------
+// ordered commit (InscyNodeCpu.cu:159-235)
+// ---------------------------------------------------------------------------
+void Engine::replay(int ci) {
+  // copy what is needed: calls_ may not grow here, but keep indices stable
+  const int f = calls_[ci].f;
+  const uint64_t rmask = calls_[ci].rmask;
+  const int depth = __builtin_popcountll(rmask);
+  std::vector<int>& V = vbuf_[depth];
+  if (V.empty()) V.assign(n_, -1);
+  std::vector<int> touched;
+  size_t ri = 0;
+  const size_t nreg = calls_[ci].regions.size();
+  for (int D = f; D < d_; ++D) {
+    const uint64_t smask = rmask | (1ull << D);
+    int nlabels = 0;
+    touched.clear();
+    while (ri < nreg && calls_[ci].regions[ri].dim == D) {
+      const HRegion R = calls_[ci].regions[ri++];
+      if (!R.passed) continue;
+      replay(R.child);
+      if (prune_redundancy(calls_[R.child], smask)) cluster_into(calls_[R.child], V, touched, nlabels);
+    }
+    join(V, touched, nlabels, smask);
+    for (int p : touched) V[p] = -1;
+  }
+}
+
+// pruneRedundancy (ScyTreeNode.cu:669-734): over result entries whose
+// subspace contains S, the smallest cluster touching the region's points;
+// the largest of these must stay below |region| * r.
+bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
+  const int* pts = levels_[c.level].pts.data() + c.pts_off;
+  int max_min = 0;
+  for (auto& e : result_) {
+    const Entry& H = e.second;
+    if ((H.mask & smask) != smask) continue;
+    int mn = -1;
+    for (int j = 0; j < c.npts; ++j) {
+      int p = pts[j];
+      if (H.lab[p] >= 0 && (mn == -1 || H.szp[p] < mn)) mn = H.szp[p];
+    }
+    if (mn > max_min) max_min = mn;
+  }
+  if (max_min == 0) return true;
+  return (double)((float)c.npts * hp_.r) > (double)max_min * 1.0;
+}
+
+// BFS numbering of INSCYClusteringImplCPUAll (ClusteringCpu.cu:317-389):
+// components in the order their first dense seed appears, members get the
+// next label, non-dense neighbours that are still -1 become -2.
+void Engine::cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>& touched, int& nlabels) {
+  const HSub& hs = subs_[c.csub];
+  const int* order = levels_[c.level].order.data() + c.pts_off;
+  for (int t = 0; t < c.norder; ++t) {
+    int comp = order[t];
+    long long m0 = hs.moff[comp], m1 = hs.moff[comp + 1];
+    if (m1 == m0) continue;
+    if (V[hs.members[m0]] != -1) continue;  // already numbered in this dim loop
+    int label = ++nlabels;
+    for (long long k = m0; k < m1; ++k) {
+      int p = hs.members[k];
+      V[p] = label;
+      touched.push_back(p);
+    }
+    for (long long k = hs.boff[comp]; k < hs.boff[comp + 1]; ++k) {
+      int q = hs.borders[k];
+      if (V[q] == -1) {
+        V[q] = -2;
+        touched.push_back(q);
+      }
+    }
+  }
+}
+
+// join (util.cu:655-743)
+void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, uint64_t smask) {
+  if (nlabels == 0) return;
+  std::vector<int> sizes(nlabels + 1, 0);
+  for (int p : touched)
+    if (V[p] >= 0) sizes[V[p]]++;
+  bool any = false;
+  for (int p : touched)
+    if (V[p] >= 0) {
+      if (sizes[V[p]] < hp_.min_size)
+        V[p] = -1;
+      else
+        any = true;
+    }
+  if (!any) return;
+  std::vector<char> drop(nlabels + 1, 0);
+  for (auto& e : result_) {
+    const Entry& H = e.second;
+    if ((H.mask & smask) != smask) continue;
+    bool hit = false;
+    for (int p : touched) {
+      int c = V[p];
+      if (c >= 0 && H.lab[p] >= 0 && (float)sizes[c] * hp_.r < (float)H.szp[p]) {
+        drop[c] = 1;
+        hit = true;
+      }
+    }
+    if (hit)
+      for (int p : touched)
+        if (V[p] >= 0 && drop[V[p]]) V[p] = -1;
+  }
+  any = false;
+  for (int p : touched)
+    if (V[p] >= 0) any = true;
+  if (!any) return;
+  std::vector<int> key = dims_of(smask);
+  auto it = result_.find(key);
+  Entry* E;
+  if (it != result_.end()) {
+    E = &it->second;
+    const int m = E->maxv;
+    for (int p : touched) {
+      if (V[p] == -2)
+        E->lab[p] = -2;
+      else if (V[p] >= 0)
+        E->lab[p] = m + 1 + V[p];
+    }
+  } else {
+    Entry ne;
+    ne.mask = smask;
+    ne.lab.assign(n_, -1);
+    for (int p : touched) ne.lab[p] = V[p];
+    E = &result_.emplace(key, std::move(ne)).first->second;
+  }
+  // refresh the entry's max label and per-point cluster sizes
+  int mx = -100000;
+  for (int v : E->lab) mx = std::max(mx, v);
+  E->maxv = mx;
+  std::vector<int> cnt(std::max(mx, 0) + 1, 0);
+  for (int v : E->lab)
+    if (v >= 0) cnt[v]++;
+  E->szp.assign(n_, 0);
+  for (long long i = 0; i < n_; ++i)
+    if (E->lab[i] >= 0) E->szp[i] = cnt[E->lab[i]];
+}
+
+}  // namespace inscy
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+struct inscy_result {
+  long long n = 0;
+  std::vector<std::vector<int>> dims;
+  std::vector<std::vector<int>> labels;
+  inscy_stats stats;
+};
+
+namespace {
+thread_local std::string g_err;
+thread_local std::unique_ptr<inscy::Engine> g_engine;
+thread_local int g_engine_device = -1;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int check_params(int64_t n, int d, const inscy_params* p) {
+  if (!p) return fail(INSCY_ERR_ARG, "params is NULL");
+  if (n < 0) return fail(INSCY_ERR_ARG, "n < 0");
+  if (n > 0x7fffffffLL) return fail(INSCY_ERR_LIMIT, "n > 2^31-1");
+  if (d <= 0) return fail(INSCY_ERR_ARG, "d <= 0");
+  if (d > 64) return fail(INSCY_ERR_LIMIT, "d > 64 (subspaces are 64-bit masks)");
+  if (!(p->neighborhood_size > 0.f)) return fail(INSCY_ERR_ARG, "neighborhood_size must be > 0");
+  if (p->number_of_cells <= 0) return fail(INSCY_ERR_ARG, "number_of_cells must be > 0");
+  if (p->number_of_cells > 255) return fail(INSCY_ERR_LIMIT, "number_of_cells > 255");
+  if (p->entropy_order != 0)
+    return fail(INSCY_ERR_UNSUPPORTED, "entropy_order != 0 is not implemented on the GPU path");
+  return INSCY_OK;
+}
+
+int run_common(const float* X, bool on_device, int64_t n, int d, const inscy_params* p, void* stream,
+               inscy_result** out) {
+  if (!out) return fail(INSCY_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  int rc = check_params(n, d, p);
+  if (rc) return rc;
+  if (n > 0 && !X) return fail(INSCY_ERR_ARG, "X is NULL");
+  if (!on_device) {
+    for (long long i = 0; i < (long long)n * d; ++i)
+      if (!(X[i] >= 0.f && X[i] <= 1.f)) return fail(INSCY_ERR_ARG, "X has a value outside [0, 1] (index " + std::to_string(i) + ")");
+  }
+  try {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (!g_engine || g_engine_device != dev) {
+      g_engine.reset(new inscy::Engine());
+      g_engine_device = dev;
+    }
+    inscy::HostParams hp;
+    hp.eps = p->neighborhood_size;
+    hp.F = p->F;
+    hp.r = p->r;
+    hp.num_obj = p->num_obj;
+    hp.min_size = p->min_size;
+    hp.cells = p->number_of_cells;
+    hp.rect = p->rectangular ? 1 : 0;
+    std::unique_ptr<inscy_result> res(new inscy_result());
+    res->n = n;
+    g_engine->run(X, on_device, n, d, hp, (cudaStream_t)stream, res->dims, res->labels, res->stats);
+    *out = res.release();
+    g_err.clear();
+    return INSCY_OK;
+  } catch (const inscy::Error& e) {
+    return fail(e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(INSCY_ERR_CUDA, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(INSCY_ERR_INTERNAL, e.what());
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int inscy_run(const float* X, int64_t n, int d, const inscy_params* p, int mode, inscy_result** out) {
+  (void)mode;
+  return run_common(X, false, n, d, p, nullptr, out);
+}
+
+int inscy_run_device(const float* X_dev, int64_t n, int d, const inscy_params* p, int mode, void* stream,
+                     inscy_result** out) {
+  (void)mode;
+  return run_common(X_dev, true, n, d, p, stream, out);
+}
+
+int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, int count, const inscy_params* p,
+                    int mode, inscy_result** outs) {
+  if (count < 0 || (count > 0 && (!Xs || !ns || !ds || !outs))) return fail(INSCY_ERR_ARG, "bad batch arguments");
+  for (int i = 0; i < count; ++i) outs[i] = nullptr;
+  for (int i = 0; i < count; ++i) {
+    int rc = inscy_run(Xs[i], ns[i], ds[i], p, mode, &outs[i]);
+    if (rc) {
+      for (int j = 0; j < i; ++j) {
+        delete outs[j];
+        outs[j] = nullptr;
+      }
+      return rc;
+    }
+  }
+  return INSCY_OK;
+}
+
+int inscy_result_count(const inscy_result* r) { return r ? (int)r->dims.size() : 0; }
+int64_t inscy_result_n(const inscy_result* r) { return r ? r->n : 0; }
+
+int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap) {
+  if (!r || i < 0 || i >= (int)r->dims.size()) return -1;
+  const auto& v = r->dims[i];
+  for (int k = 0; k < (int)v.size() && k < cap; ++k) dims[k] = v[k];
+  return (int)v.size();
+}
+
+int inscy_result_labels(const inscy_result* r, int i, int32_t* out) {
+  if (!r || !out || i < 0 || i >= (int)r->labels.size()) return fail(INSCY_ERR_ARG, "bad result index");
+  std::memcpy(out, r->labels[i].data(), sizeof(int32_t) * r->labels[i].size());
+  return INSCY_OK;
+}
+
+int inscy_result_stats(const inscy_result* r, inscy_stats* out) {
+  if (!r || !out) return fail(INSCY_ERR_ARG, "NULL argument");
+  *out = r->stats;
+  return INSCY_OK;
+}
+
+void inscy_result_free(inscy_result* r) { delete r; }
+
+const char* inscy_last_error(void) { return g_err.c_str(); }
+
+const char* inscy_version(void) { return "inscy_gb300 0.1"; }
+
+}  // extern "C"

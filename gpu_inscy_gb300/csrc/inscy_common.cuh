@@ -1,0 +1,93 @@
+// Shared device-side types and helpers of the GB300 INSCY engine.
+//
+// Terminology (follows the reference, mrjakobdk/GPU_INSCY):
+//   * coarse cell  -- the SCY-tree grid cell, min(int(x / (1/cells)), cells-1)
+//                     (ScyTreeNode.cu:100-102);
+//   * fine cell    -- the same rule on the ceil(1/eps) grid of the
+//                     neighbourhood tree (inscy_map.cpp:243);
+//   * ghost        -- an s-connection chain (ScyTreeNode.cu:34-49): point p
+//                     owns one on dim k when x[p][k] >= (cell+1)/cells - eps;
+//   * subspace     -- a set of restricted dims, always restricted in
+//                     ascending order, kept as a 64-bit mask;
+//   * call         -- one INSCY recursion node (InscyNodeCpu.cu:159-235):
+//                     a restricted, merged and pruned SCY-tree;
+//   * region       -- one restriction of a call to (dim, run of cells), after
+//                     mergeWithNeighbors (ScyTreeNode.cu:837-851).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace inscy {
+
+constexpr int kMaxDims = 64;    // subspaces are 64-bit masks
+constexpr int kMaxCells = 255;  // coarse cells fit a byte
+constexpr int kWarp = 32;
+
+// Region record written by the level kernel (one per restriction run).
+struct RegionRec {
+  int call;       // index of the parent call in its level
+  int dim;        // restricted dim
+  int c0, c1;     // run of merged cells [c0, c1]
+  int npts;       // points left after the weak-density prune
+  int passed;     // npts >= min_size: the region recurses (becomes a call)
+  long long pts_off;    // where its pruned points were written (passed only)
+  long long ghost_off;  // where its detached ghosts were written (passed only)
+  int nghost;
+  int pad;
+};
+
+// One call of the level being expanded (device view).
+struct CallDesc {
+  long long pts_off;    // points, in the call's leaf order
+  long long ghost_off;  // detached ghosts: (point, dim) pairs
+  uint64_t rmask;       // restricted dims
+  int npts;
+  int f;                // first dim the call restricts (InscyNodeCpu.cu:172)
+  int nghost;
+  int sub;              // the call's subspace in the previous level (-1: root)
+  int child_sub;        // first child subspace (dim f) in the current level
+  int nrestricted;
+};
+
+// A subspace whose density is evaluated at the current level.
+struct SubDesc {
+  uint64_t mask;      // dims of the subspace
+  int dim;            // its largest dim (the one added at this level)
+  int nsub;           // |S|
+  int parent;         // parent subspace in the previous level (-1 at level 1)
+  int nquery;         // query points = kept points of the parent (all points at level 1)
+  long long item_off;   // first work item of this subspace
+  long long query_off;  // parent's kept-point list offset (level 1: unused)
+  long long plist_base; // parent's list base (entry offsets are absolute)
+  long long bitmap_off; // word offset of this subspace's flag bitmaps
+};
+
+// Per-point flag bits of a (subspace, point) evaluation.
+enum : uint8_t { kFlagWeak = 1, kFlagDense = 2, kFlagKeep = 4 };
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Squared-distance step of dist() (ClusteringCpu.cu:40-50): acc + diff*diff
+// with each operation rounded separately (no fused multiply-add).
+__device__ __forceinline__ float dist_step(float acc, float xp, float xq) {
+  float diff = __fsub_rn(xp, xq);
+  return __fadd_rn(acc, __fmul_rn(diff, diff));
+}
+
+// phi() term (ClusteringCpu.cu:118-120): d = dist/eps; sq = d*d; the float
+// sum absorbs (1. - sq) through a double addition, then rounds to float.
+__device__ __forceinline__ double phi_term(float dist, float eps) {
+  float dd = __fdiv_rn(dist, eps);
+  float sq = __fmul_rn(dd, dd);
+  return __dsub_rn(1.0, (double)sq);
+}
+__device__ __forceinline__ float phi_add(float sum, double term) {
+  return __double2float_rn(__dadd_rn((double)sum, term));
+}
+
+}  // namespace inscy

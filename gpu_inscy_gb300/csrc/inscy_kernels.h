@@ -1,0 +1,128 @@
+// Launchers of the engine's kernels (host-callable, C++ linkage).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "inscy_common.cuh"
+
+namespace inscy {
+
+// ---- primitives / setup (kernels_setup.cu)
+void launch_exclusive_scan_int(const int* in, int* out, long long n, int* total, void* sums, cudaStream_t s);
+void launch_exclusive_scan_ll(const long long* in, long long* out, long long n, long long* total, void* sums,
+                              cudaStream_t s);
+void launch_exclusive_scan_i2ll(const int* in, long long* out, long long n, long long* total, void* sums,
+                                cudaStream_t s);
+void launch_prep(const float* X, int n, int d, int cells, float csz, int G, float fsz, float eps, uint8_t* cc,
+                 uint8_t* fc, unsigned long long* gz, cudaStream_t s);
+void launch_iota(int* a, int n, cudaStream_t s);
+void launch_check_range(const float* X, long long m, int* bad, cudaStream_t s);
+void launch_scatter_rank(const int* order, int n, int* rank, cudaStream_t s);
+void launch_byte_sort_pass(const int* in, int* out, int m, const uint8_t* bytes, int d, int k, int* hist,
+                           int* hist_total, int* digit_start, void* sums, cudaStream_t s);
+void launch_digit_starts(const int* hist, int nb, int m, int* starts, cudaStream_t s);
+void launch_candidate_lists(int n, int d, int G, const int* bucket_pts, const int* bucket_off, const int* rank,
+                            const uint8_t* fc, const long long* list_off, int* list_pts, cudaStream_t s);
+
+// ---- density (kernels_density.cu)
+struct DensityLaunch {
+  const SubDesc* subs;
+  int nsubs;
+  long long nitems;
+  const float* X;
+  const uint8_t* fc;
+  int n, d, G;
+  float eps;
+  int rect;
+  float thr_weak;
+  const float* thr_dense;
+  const float* thr_keep;
+  const long long* cand_off;
+  const int* cand_pts;
+  const int* prev_keep;
+  const long long* prev_loff;
+  const int* prev_lcnt;
+  const int* prev_lids;
+  const float* prev_lacc;
+  int* cnt;
+  uint8_t* flags;
+  unsigned* bitmaps;
+  int words;
+  const long long* out_off;
+  int* out_ids;
+  float* out_acc;
+};
+void launch_density(const DensityLaunch& L, bool write, cudaStream_t s);
+void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
+                        cudaStream_t s);
+void launch_keep_compact(const SubDesc* subs, int nsubs, long long nitems, const uint8_t* flags, const int* cnt,
+                         const long long* kpos, const long long* loff, const int* prev_keep, int* keep_ids,
+                         long long* keep_loff, int* keep_lcnt, cudaStream_t s);
+void launch_word_popc(const unsigned* words, long long nw, int* out, cudaStream_t s);
+void launch_gather_kstart(const SubDesc* subs, int nsubs, const long long* kpos, long long nitems, long long K,
+                          long long* out, cudaStream_t s);
+void launch_gather_cbase(const long long* kstart, int nsubs, const int* root_id, long long K, int ncomp, int* out,
+                         cudaStream_t s);
+
+// ---- SCY-tree level (kernels_tree.cu)
+struct TreeLaunch {
+  const CallDesc* calls;
+  int ncalls;
+  const long long* work_off;
+  int nwork;
+  const int* pts_in;
+  const int2* ghosts_in;
+  const uint8_t* cc;
+  const unsigned long long* gz;
+  int n, d, cells, min_size;
+  const SubDesc* subs;
+  const unsigned* bitmaps;
+  int* scratch;
+  const long long* work_scratch;
+  RegionRec* recs;
+  int* nrecs;
+  int* out_pts;
+  unsigned long long* out_pts_top;
+  long long out_pts_cap;
+  int2* out_ghosts;
+  unsigned long long* out_ghost_top;
+  long long out_ghost_cap;
+  int* err;
+};
+void launch_tree_level(const TreeLaunch& L, cudaStream_t s);
+
+// ---- clustering (kernels_cluster.cu)
+struct ClusterArgs {
+  int nsubs;
+  const SubDesc* subs;
+  const long long* kstart;  // [nsubs + 1] first kept index of each subspace
+  const int* keep_ids;
+  const long long* keep_loff;
+  const int* keep_lcnt;
+  const int* lids;
+  const unsigned* bitmaps;
+  int words;
+  const int* keep_word_rank;  // [nsubs * words] global prefix of kept popcounts
+  const uint8_t* clustered;   // [nsubs]
+  const int* clustered_list;  // [nclustered] subspace of each clustered slot
+  long long nkeep;
+  int n;
+  int* uf;
+  int* err;
+};
+void launch_uf_init(int* par, long long n, cudaStream_t s);
+void launch_uf_union(const ClusterArgs& a, cudaStream_t s);
+void launch_uf_flatten(const ClusterArgs& a, int* is_root, cudaStream_t s);
+void launch_comp_ids(const ClusterArgs& a, const int* root_id, int* comp, int* mcount, cudaStream_t s);
+void launch_members(const ClusterArgs& a, const int* comp, const long long* moff, int* mfill, int* members,
+                    cudaStream_t s);
+void launch_borders(const ClusterArgs& a, const int* comp, const int* cslot_of, int* slots, int2* ovf, int* novf,
+                    int ovf_cap, cudaStream_t s);
+void launch_border_count(const int* slots, long long nslots2, const int2* ovf, int novf, int* bcount, cudaStream_t s);
+void launch_border_fill(const int* slots, long long nslots2, int n, const int2* ovf, int novf, const long long* boff,
+                        int* bfill, int* borders, cudaStream_t s);
+void launch_region_order(const ClusterArgs& a, int nclustered, const int* comp, const int* cbase_of,
+                         const int* sub_calls_off, const int* sub_calls, const CallDesc* ncalls, const int* pts,
+                         int* firstpos, int* order, int* order_cnt, cudaStream_t s);
+
+}  // namespace inscy

@@ -1,0 +1,314 @@
+// Clustering of the subspaces of one level (INSCYClusteringImplCPUAll,
+// ClusteringCpu.cu:317-389, re-derived).
+//
+// The reference runs a BFS from every region point in leaf order: a dense
+// point joins the current cluster and enqueues its unvisited neighbours
+// (marking them -2), a non-dense point ends the branch.  Since the neighbour
+// relation is symmetric and density is a pure function of (point, subspace),
+// the outcome is:
+//   * clusters  = connected components of the dense points under the
+//                 neighbour relation, numbered in the order in which the
+//                 region's leaf order first meets a dense point of each;
+//   * -2 marks  = non-dense points adjacent to a dense point of a numbered
+//                 component.
+// So the GPU computes, per subspace, the components (lock-free atomicCAS
+// union-find with pointer jumping), per component its members and its
+// non-dense border points, and per region the components in first-seed order.
+// The host then numbers them exactly as the BFS does.
+#include <climits>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "inscy_common.cuh"
+#include "inscy_prims.cuh"
+#include "inscy_kernels.h"
+
+namespace inscy {
+
+constexpr int kUnionLimit = 1 << 22;  // bound on CAS retries of one union
+
+__device__ __forceinline__ bool bit_of(const unsigned* bm, int p) { return (bm[p >> 5] >> (p & 31)) & 1u; }
+
+// global keep index of point q in subspace si (rank in its keep bitmap)
+__device__ __forceinline__ long long keep_index(const ClusterArgs& a, int si, int q) {
+  const unsigned* kb = a.bitmaps + a.subs[si].bitmap_off + 2LL * a.words;
+  unsigned wv = kb[q >> 5];
+  return (long long)a.keep_word_rank[(long long)si * a.words + (q >> 5)] + __popc(wv & ((1u << (q & 31)) - 1u));
+}
+
+__device__ __forceinline__ int find_sub_by_keep(const long long* kstart, int nsubs, long long kk) {
+  int lo = 0, hi = nsubs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (kstart[mid] <= kk)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int uf_find(int* par, int x) {
+  volatile int* vp = par;
+  int cur = x;
+  int next = vp[cur];
+  int guard = 0;
+  while (next != cur) {
+    int nn = vp[next];
+    if (nn != next) vp[cur] = nn;  // path halving: only ever points closer to the root
+    cur = next;
+    next = vp[cur];
+    if (++guard > kUnionLimit) break;
+  }
+  return cur;
+}
+
+__device__ __forceinline__ void uf_unite(int* par, int a, int b, int* err) {
+  int ra = uf_find(par, a), rb = uf_find(par, b);
+  int it = 0;
+  while (ra != rb) {
+    if (ra < rb) {
+      int t = ra;
+      ra = rb;
+      rb = t;
+    }
+    int old = atomicCAS(&par[ra], ra, rb);  // hook the larger root under the smaller
+    if (old == ra) return;
+    ra = uf_find(par, old);
+    rb = uf_find(par, rb);
+    if (++it > kUnionLimit) {
+      atomicExch(err, 3);
+      return;
+    }
+  }
+}
+
+__global__ void k_uf_init(int* par, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) par[i] = (int)i;
+}
+
+// one warp per kept point of a clustered subspace
+__global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a) {
+  const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (kk >= a.nkeep) return;
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  if (!a.clustered[si]) return;
+  const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+  const int p = a.keep_ids[kk];
+  if (!bit_of(dn, p)) return;
+  const long long b = a.keep_loff[kk];
+  const int len = a.keep_lcnt[kk];
+  for (int j = lane_id(); j < len; j += 32) {
+    int q = a.lids[b + j];
+    if (!bit_of(dn, q)) continue;
+    long long kq = keep_index(a, si, q);
+    if (kq < kk) uf_unite(a.uf, (int)kk, (int)kq, a.err);
+  }
+}
+
+// flatten: every dense point points at its root; roots are flagged
+__global__ void k_uf_flatten(ClusterArgs a, int* is_root) {
+  long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  int root = 0;
+  if (a.clustered[si]) {
+    const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+    if (bit_of(dn, a.keep_ids[kk])) {
+      int r = uf_find(a.uf, (int)kk);
+      a.uf[kk] = r;
+      root = (r == (int)kk);
+    }
+  }
+  is_root[kk] = root;
+}
+
+// component id (global, dense) of every dense kept point; -1 otherwise
+__global__ void k_comp_ids(ClusterArgs a, const int* __restrict__ root_id, int* __restrict__ comp,
+                           int* __restrict__ mcount) {
+  long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  int c = -1;
+  if (a.clustered[si]) {
+    const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+    if (bit_of(dn, a.keep_ids[kk])) {
+      c = root_id[a.uf[kk]];
+      atomicAdd(&mcount[c], 1);
+    }
+  }
+  comp[kk] = c;
+}
+
+__global__ void k_members(ClusterArgs a, const int* __restrict__ comp, const long long* __restrict__ moff,
+                          int* __restrict__ mfill, int* __restrict__ members) {
+  long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  int c = comp[kk];
+  if (c < 0) return;
+  int o = atomicAdd(&mfill[c], 1);
+  members[moff[c] + o] = a.keep_ids[kk];
+}
+
+// border pairs (component, non-dense neighbour), de-duplicated through two
+// slots per (clustered subspace, point); rare third components overflow
+__global__ void __launch_bounds__(256) k_borders(ClusterArgs a, const int* __restrict__ comp,
+                                                 const int* __restrict__ cslot_of, int* __restrict__ slots,
+                                                 int2* __restrict__ ovf, int* __restrict__ novf, int ovf_cap) {
+  const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (kk >= a.nkeep) return;
+  const int c = comp[kk];
+  if (c < 0) return;
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+  const long long b = a.keep_loff[kk];
+  const int len = a.keep_lcnt[kk];
+  int* sl = slots + (long long)cslot_of[si] * a.n * 2;
+  for (int j = lane_id(); j < len; j += 32) {
+    int q = a.lids[b + j];
+    if (bit_of(dn, q)) continue;
+    int* s2 = sl + 2LL * q;
+    int v0 = ((volatile int*)s2)[0];
+    if (v0 == c) continue;
+    if (v0 == -1) {
+      int old = atomicCAS(&s2[0], -1, c);
+      if (old == -1 || old == c) continue;
+    }
+    int v1 = ((volatile int*)s2)[1];
+    if (v1 == c) continue;
+    if (v1 == -1) {
+      int old = atomicCAS(&s2[1], -1, c);
+      if (old == -1 || old == c) continue;
+    }
+    int o = atomicAdd(novf, 1);
+    if (o < ovf_cap)
+      ovf[o] = make_int2(c, q);
+    else
+      atomicExch(a.err, 4);
+  }
+}
+
+__global__ void k_border_count(const int* __restrict__ slots, long long nslots2, int* __restrict__ bcount) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nslots2) return;
+  int c = slots[i];
+  if (c >= 0) atomicAdd(&bcount[c], 1);
+}
+
+__global__ void k_border_count_ovf(const int2* __restrict__ ovf, int novf, int* __restrict__ bcount) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < novf) atomicAdd(&bcount[ovf[i].x], 1);
+}
+
+__global__ void k_border_fill(const int* __restrict__ slots, long long nslots2, int n, const long long* __restrict__ boff,
+                              int* __restrict__ bfill, int* __restrict__ borders) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nslots2) return;
+  int c = slots[i];
+  if (c < 0) return;
+  int q = (int)((i >> 1) % n);
+  int o = atomicAdd(&bfill[c], 1);
+  borders[boff[c] + o] = q;
+}
+
+__global__ void k_border_fill_ovf(const int2* __restrict__ ovf, int novf, const long long* __restrict__ boff,
+                                  int* __restrict__ bfill, int* __restrict__ borders) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= novf) return;
+  int2 e = ovf[i];
+  int o = atomicAdd(&bfill[e.x], 1);
+  borders[boff[e.x] + o] = e.y;
+}
+
+// Components of each region in first-dense-seed order.  One block per
+// clustered subspace walks its regions (they may share components).
+__global__ void __launch_bounds__(256) k_region_order(ClusterArgs a, const int* __restrict__ comp,
+                                                      const int* __restrict__ cbase_of,
+                                                      const int* __restrict__ sub_calls_off,
+                                                      const int* __restrict__ sub_calls, const CallDesc* __restrict__ ncalls,
+                                                      const int* __restrict__ pts, int* __restrict__ firstpos,
+                                                      int* __restrict__ order, int* __restrict__ order_cnt) {
+  __shared__ int sh[32];
+  const int cs = blockIdx.x;  // clustered-subspace slot
+  const int si = a.clustered_list[cs];
+  const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+  const int cb = cbase_of[si];
+  for (int t = sub_calls_off[cs]; t < sub_calls_off[cs + 1]; ++t) {
+    const int call = sub_calls[t];
+    const CallDesc C = ncalls[call];
+    const int* P = pts + C.pts_off;
+    const int m = C.npts;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      int p = P[j];
+      if (bit_of(dn, p)) atomicMin(&firstpos[comp[keep_index(a, si, p)]], j);
+    }
+    __syncthreads();
+    int base = 0;
+    for (int c0 = 0; c0 < m; c0 += blockDim.x) {
+      int j = c0 + threadIdx.x;
+      int f = 0, c = -1;
+      if (j < m) {
+        int p = P[j];
+        if (bit_of(dn, p)) {
+          c = comp[keep_index(a, si, p)];
+          f = firstpos[c] == j;
+        }
+      }
+      int tot;
+      int inc = block_inclusive_scan<int>(f, sh, &tot);
+      if (f) order[C.pts_off + base + inc - 1] = c - cb;
+      base += tot;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      int p = P[j];
+      if (bit_of(dn, p)) firstpos[comp[keep_index(a, si, p)]] = INT_MAX;
+    }
+    if (threadIdx.x == 0) order_cnt[call] = base;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+void launch_uf_init(int* par, long long n, cudaStream_t s) {
+  if (n > 0) k_uf_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(par, n);
+}
+void launch_uf_union(const ClusterArgs& a, cudaStream_t s) {
+  if (a.nkeep > 0) k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a);
+}
+void launch_uf_flatten(const ClusterArgs& a, int* is_root, cudaStream_t s) {
+  if (a.nkeep > 0) k_uf_flatten<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, is_root);
+}
+void launch_comp_ids(const ClusterArgs& a, const int* root_id, int* comp, int* mcount, cudaStream_t s) {
+  if (a.nkeep > 0) k_comp_ids<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, root_id, comp, mcount);
+}
+void launch_members(const ClusterArgs& a, const int* comp, const long long* moff, int* mfill, int* members,
+                    cudaStream_t s) {
+  if (a.nkeep > 0) k_members<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, comp, moff, mfill, members);
+}
+void launch_borders(const ClusterArgs& a, const int* comp, const int* cslot_of, int* slots, int2* ovf, int* novf,
+                    int ovf_cap, cudaStream_t s) {
+  if (a.nkeep > 0)
+    k_borders<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a, comp, cslot_of, slots, ovf, novf, ovf_cap);
+}
+void launch_border_count(const int* slots, long long nslots2, const int2* ovf, int novf, int* bcount,
+                         cudaStream_t s) {
+  if (nslots2 > 0) k_border_count<<<(unsigned)((nslots2 + 255) / 256), 256, 0, s>>>(slots, nslots2, bcount);
+  if (novf > 0) k_border_count_ovf<<<(novf + 255) / 256, 256, 0, s>>>(ovf, novf, bcount);
+}
+void launch_border_fill(const int* slots, long long nslots2, int n, const int2* ovf, int novf, const long long* boff,
+                        int* bfill, int* borders, cudaStream_t s) {
+  if (nslots2 > 0)
+    k_border_fill<<<(unsigned)((nslots2 + 255) / 256), 256, 0, s>>>(slots, nslots2, n, boff, bfill, borders);
+  if (novf > 0) k_border_fill_ovf<<<(novf + 255) / 256, 256, 0, s>>>(ovf, novf, boff, bfill, borders);
+}
+void launch_region_order(const ClusterArgs& a, int nclustered, const int* comp, const int* cbase_of,
+                         const int* sub_calls_off, const int* sub_calls, const CallDesc* ncalls, const int* pts,
+                         int* firstpos, int* order, int* order_cnt, cudaStream_t s) {
+  if (nclustered > 0)
+    k_region_order<<<nclustered, 256, 0, s>>>(a, comp, cbase_of, sub_calls_off, sub_calls, ncalls, pts, firstpos,
+                                              order, order_cnt);
+}
+
+}  // namespace inscy

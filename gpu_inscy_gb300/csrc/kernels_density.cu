@@ -1,0 +1,281 @@
+// epsilon-neighbourhood density of every (subspace, point) of one lattice level.
+//
+// Reference semantics (ClusteringCpu.cu:40-125, ScyTreeNode.cu:896-946):
+//   * candidates of p in subspace S are the points whose fine cells are within
+//     +-1 of p's on every dim of S, in neighbourhood-trie order;
+//   * q != p is a neighbour when eps >= sqrt(sum over S, ascending, of
+//     (p_k - q_k)^2), every operation rounded separately;
+//   * phi(p) = sum over neighbours, in candidate order, of (1 - (dist/eps)^2)
+//     accumulated in float through a double addition;
+//   * dense / weak-dense / rectangular tests compare phi (or the neighbour
+//     count) with host-computed float thresholds.
+//
+// Because subspaces are extended by their largest dim D, N(p, S u {D}) is the
+// ordered subsequence of N(p, S) that passes the +-1 test on D and the
+// distance test; the partial squared distance is stored with each list entry
+// so a child adds exactly one term, in the reference's summation order.
+// Level-1 subspaces {D} read the precomputed candidate list of p's fine cell.
+//
+// One warp per (subspace, query point); candidates are consumed 32 at a time
+// with a ballot, and phi is accumulated over the accepted lanes in order.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "inscy_common.cuh"
+#include "inscy_kernels.h"
+
+namespace inscy {
+
+struct DensityArgs {
+  const SubDesc* subs;
+  int nsubs;
+  long long nitems;
+  const float* X;
+  const uint8_t* fc;
+  int n, d, G;
+  float eps;
+  int rect;
+  float thr_weak;
+  const float* thr_dense;  // [|S|]
+  const float* thr_keep;   // [|S|]
+  // level-1 candidate lists
+  const long long* cand_off;  // d*G + 1
+  const int* cand_pts;
+  // previous level (parent subspaces): kept points and their lists
+  const int* prev_keep;
+  const long long* prev_loff;
+  const int* prev_lcnt;
+  const int* prev_lids;
+  const float* prev_lacc;
+  // outputs
+  int* cnt;                 // [nitems]
+  uint8_t* flags;           // [nitems]
+  unsigned* bitmaps;        // per subspace 3 * W words (weak, dense, keep)
+  int words;                // W = ceil(n / 32)
+  // pass 2 (list output)
+  const long long* out_off;  // [nitems] list start of kept items
+  int* out_ids;
+  float* out_acc;
+};
+
+__device__ __forceinline__ int find_sub(const SubDesc* subs, int nsubs, long long item) {
+  int lo = 0, hi = nsubs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (subs[mid].item_off <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+template <bool kWrite>
+__global__ void __launch_bounds__(256) k_density(DensityArgs a) {
+  const long long item = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (item >= a.nitems) return;
+  const unsigned lane = lane_id();
+  const int si = find_sub(a.subs, a.nsubs, item);
+  const SubDesc S = a.subs[si];
+  const long long i = item - S.item_off;
+  const bool level1 = S.parent < 0;
+  if (kWrite && !(a.flags[item] & kFlagKeep)) return;
+
+  const int D = S.dim;
+  const int p = level1 ? (int)i : a.prev_keep[S.query_off + i];
+  const float xp = a.X[(size_t)p * a.d + D];
+  const int fp = a.fc[(size_t)p * a.d + D];
+  const int* ids;
+  const float* accs = nullptr;
+  long long len;
+  if (level1) {
+    long long b = a.cand_off[(size_t)D * a.G + fp], e = a.cand_off[(size_t)D * a.G + fp + 1];
+    ids = a.cand_pts + b;
+    len = e - b;
+  } else {
+    long long b = a.prev_loff[S.query_off + i];
+    ids = a.prev_lids + b;
+    accs = a.prev_lacc + b;
+    len = a.prev_lcnt[S.query_off + i];
+  }
+
+  float sum = 0.f;
+  int count = 0;
+  long long wbase = kWrite ? a.out_off[item] : 0;
+  for (long long j0 = 0; j0 < len; j0 += 32) {
+    long long j = j0 + lane;
+    bool ok = j < len;
+    int q = ok ? ids[j] : -1;
+    ok = ok && q != p;
+    if (ok && !level1) {
+      int fq = a.fc[(size_t)q * a.d + D];
+      ok = fq >= fp - 1 && fq <= fp + 1;
+    }
+    float acc2 = 0.f, dist = 0.f;
+    if (ok) {
+      float acc = level1 ? 0.f : accs[j];
+      acc2 = dist_step(acc, xp, a.X[(size_t)q * a.d + D]);
+      dist = __fsqrt_rn(acc2);
+      ok = a.eps >= dist;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (kWrite) {
+      if (ok) {
+        long long o = wbase + count + __popc(m & lanemask_lt());
+        a.out_ids[o] = q;
+        a.out_acc[o] = acc2;
+      }
+    } else if (!a.rect) {
+      double t = ok ? phi_term(dist, a.eps) : 0.0;
+      unsigned mm = m;
+      while (mm) {
+        int b = __ffs(mm) - 1;
+        mm &= mm - 1;
+        double tb = __shfl_sync(0xffffffffu, t, b);
+        sum = phi_add(sum, tb);
+      }
+    }
+    count += __popc(m);
+  }
+  if (kWrite) return;
+  const float v = a.rect ? (float)count : sum;
+  uint8_t f = 0;
+  if (v >= a.thr_weak) f |= kFlagWeak;
+  if (v >= a.thr_dense[S.nsub]) f |= kFlagDense;
+  if (v >= a.thr_keep[S.nsub]) f |= kFlagKeep;
+  if (lane == 0) {
+    a.cnt[item] = count;
+    a.flags[item] = f;
+    unsigned bit = 1u << (p & 31);
+    unsigned* bm = a.bitmaps + S.bitmap_off + (p >> 5);
+    if (f & kFlagWeak) atomicOr(bm, bit);
+    if (f & kFlagDense) atomicOr(bm + a.words, bit);
+    if (f & kFlagKeep) atomicOr(bm + 2 * a.words, bit);
+  }
+}
+
+// kept items: list lengths (0 for the others) for the offset scan
+__global__ void k_keep_counts(const int* __restrict__ cnt, const uint8_t* __restrict__ flags, long long nitems,
+                              int* __restrict__ kcnt, int* __restrict__ kflag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nitems) return;
+  bool k = flags[i] & kFlagKeep;
+  kcnt[i] = k ? cnt[i] : 0;
+  kflag[i] = k ? 1 : 0;
+}
+
+// compact the kept items into the level's kept-point arrays
+__global__ void k_keep_compact(const SubDesc* __restrict__ subs, int nsubs, long long nitems,
+                               const uint8_t* __restrict__ flags, const int* __restrict__ cnt,
+                               const long long* __restrict__ kpos, const long long* __restrict__ loff,
+                               const int* __restrict__ prev_keep, int* __restrict__ keep_ids,
+                               long long* __restrict__ keep_loff, int* __restrict__ keep_lcnt) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nitems) return;
+  if (!(flags[i] & kFlagKeep)) return;
+  int si = find_sub(subs, nsubs, i);
+  const SubDesc& S = subs[si];
+  long long li = i - S.item_off;
+  int p = S.parent < 0 ? (int)li : prev_keep[S.query_off + li];
+  long long k = kpos[i];
+  keep_ids[k] = p;
+  keep_loff[k] = loff[i];
+  keep_lcnt[k] = cnt[i];
+}
+
+// popcount of every bitmap word (for rank lookups in the keep bitmaps)
+__global__ void k_word_popc(const unsigned* __restrict__ words, long long nw, int* __restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nw) out[i] = __popc(words[i]);
+}
+
+// first kept index of every subspace: the kept-prefix at its first item
+__global__ void k_gather_kstart(const SubDesc* __restrict__ subs, int nsubs, const long long* __restrict__ kpos,
+                                long long nitems, long long K, long long* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nsubs) return;
+  if (i == nsubs) {
+    out[i] = K;
+    return;
+  }
+  long long it = subs[i].item_off;
+  out[i] = it < nitems ? kpos[it] : K;
+}
+
+// first component id of every subspace
+__global__ void k_gather_cbase(const long long* __restrict__ kstart, int nsubs, const int* __restrict__ root_id,
+                               long long K, int ncomp, int* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nsubs) return;
+  long long k = kstart[i];
+  out[i] = k < K ? root_id[k] : ncomp;
+}
+
+void launch_gather_kstart(const SubDesc* subs, int nsubs, const long long* kpos, long long nitems, long long K,
+                          long long* out, cudaStream_t s) {
+  k_gather_kstart<<<(nsubs + 1 + 255) / 256, 256, 0, s>>>(subs, nsubs, kpos, nitems, K, out);
+}
+
+void launch_gather_cbase(const long long* kstart, int nsubs, const int* root_id, long long K, int ncomp, int* out,
+                         cudaStream_t s) {
+  k_gather_cbase<<<(nsubs + 1 + 255) / 256, 256, 0, s>>>(kstart, nsubs, root_id, K, ncomp, out);
+}
+
+void launch_density(const DensityLaunch& L, bool write, cudaStream_t s) {
+  if (L.nitems <= 0) return;
+  DensityArgs a;
+  a.subs = L.subs;
+  a.nsubs = L.nsubs;
+  a.nitems = L.nitems;
+  a.X = L.X;
+  a.fc = L.fc;
+  a.n = L.n;
+  a.d = L.d;
+  a.G = L.G;
+  a.eps = L.eps;
+  a.rect = L.rect;
+  a.thr_weak = L.thr_weak;
+  a.thr_dense = L.thr_dense;
+  a.thr_keep = L.thr_keep;
+  a.cand_off = L.cand_off;
+  a.cand_pts = L.cand_pts;
+  a.prev_keep = L.prev_keep;
+  a.prev_loff = L.prev_loff;
+  a.prev_lcnt = L.prev_lcnt;
+  a.prev_lids = L.prev_lids;
+  a.prev_lacc = L.prev_lacc;
+  a.cnt = L.cnt;
+  a.flags = L.flags;
+  a.bitmaps = L.bitmaps;
+  a.words = L.words;
+  a.out_off = L.out_off;
+  a.out_ids = L.out_ids;
+  a.out_acc = L.out_acc;
+  long long threads = L.nitems * 32;
+  unsigned blocks = (unsigned)((threads + 255) / 256);
+  if (write)
+    k_density<true><<<blocks, 256, 0, s>>>(a);
+  else
+    k_density<false><<<blocks, 256, 0, s>>>(a);
+}
+
+void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
+                        cudaStream_t s) {
+  if (nitems <= 0) return;
+  k_keep_counts<<<(unsigned)((nitems + 255) / 256), 256, 0, s>>>(cnt, flags, nitems, kcnt, kflag);
+}
+
+void launch_keep_compact(const SubDesc* subs, int nsubs, long long nitems, const uint8_t* flags, const int* cnt,
+                         const long long* kpos, const long long* loff, const int* prev_keep, int* keep_ids,
+                         long long* keep_loff, int* keep_lcnt, cudaStream_t s) {
+  if (nitems <= 0) return;
+  k_keep_compact<<<(unsigned)((nitems + 255) / 256), 256, 0, s>>>(subs, nsubs, nitems, flags, cnt, kpos, loff,
+                                                                  prev_keep, keep_ids, keep_loff, keep_lcnt);
+}
+
+void launch_word_popc(const unsigned* words, long long nw, int* out, cudaStream_t s) {
+  if (nw <= 0) return;
+  k_word_popc<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(words, nw, out);
+}
+
+}  // namespace inscy

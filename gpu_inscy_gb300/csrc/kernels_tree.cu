@@ -1,0 +1,460 @@
+// SCY-tree restrict / merge / prune for every (call, dim) of one level.
+//
+// A call's SCY-tree (ScyTreeNode.h:25-121) is held as
+//   * its points, stored in the tree's leaf order (get_points,
+//     ScyTreeNode.cu:853-869): lexicographic in the cells of the remaining
+//     dims, then the cells of the restricted dims from the last restricted
+//     one back to the first, then point id;
+//   * its "detached ghosts": s-connection chains (ScyTreeNode.cu:34-49)
+//     whose point was pruned earlier but whose chain is still in the trie.
+//     The chains of points still present are implied by the per-point ghost
+//     flags.
+// Given that representation, the reference's pointer-trie operations become:
+//   restrict(D, c)            keep points with cell c on D
+//                             (ScyTreeNode.cu:227-379); a ghost whose chain
+//                             starts on D and lies in cell c marks the result
+//                             s-connected, other ghosts survive when their
+//                             point's cell on D is c;
+//   mergeWithNeighbors        absorb cell c+1 while the tree restricted last was
+//                             s-connected (ScyTreeNode.cu:837-851); the merged
+//                             leaf order is a stable sort by (remaining cells,
+//                             cell on D); when no dim remains and the first
+//                             cell is empty the absorbed points are lost, as
+//                             mergeNodes adds points only to a node whose
+//                             count is positive (ScyTreeNode.cu:805-808);
+//   pruneRecursionAndRemove2  keep weak-dense points (ScyTreeNode.cu:582-667);
+//                             propergate_count2 (:446-467) then erases empty
+//                             child nodes together with the s-connection of the
+//                             same cell, which decides which ghosts survive.
+// All of this is integer work: filters are block-wide stable compactions and
+// the merge re-sort is a stable counting-sort per dim (warp match + block
+// scan).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "inscy_common.cuh"
+#include "inscy_prims.cuh"
+#include "inscy_kernels.h"
+
+namespace inscy {
+
+constexpr int kTreeThreads = 256;
+constexpr int kTreeWarps = kTreeThreads / 32;
+
+struct TreeArgs {
+  const CallDesc* calls;
+  int ncalls;
+  const long long* work_off;  // [ncalls]: first work item of each call
+  int nwork;
+  const int* pts_in;
+  const int2* ghosts_in;
+  const uint8_t* cc;
+  const unsigned long long* gz;
+  int n, d, cells, min_size;
+  const SubDesc* subs;
+  const unsigned* bitmaps;
+  int* scratch;  // per work item: 3 * npts + 1 ints at work_scratch[w]
+  const long long* work_scratch;
+  RegionRec* recs;  // per work item: cells records
+  int* nrecs;
+  int* out_pts;
+  unsigned long long* out_pts_top;
+  long long out_pts_cap;
+  int2* out_ghosts;
+  unsigned long long* out_ghost_top;
+  long long out_ghost_cap;
+  int* err;
+};
+
+template <class Pred>
+__device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) {
+  int base = 0;
+  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+    int j = c0 + threadIdx.x;
+    int x = j < n ? in[j] : 0;
+    int f = (j < n && pred(x)) ? 1 : 0;
+    int tot;
+    int inc = block_inclusive_scan<int>(f, sh, &tot);
+    if (f) out[base + inc - 1] = x;
+    base += tot;
+  }
+  return base;
+}
+
+// one stable counting-sort pass by digit(x) in [0, R)
+template <class Dig>
+__device__ void block_sort_pass(const int* in, int* out, int n, Dig dig, int R, int* s_base, int* s_tot, int* s_wc) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < R; i += blockDim.x) s_base[i] = 0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) atomicAdd(&s_base[dig(in[j])], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int i = 0; i < R; ++i) {
+      int t = s_base[i];
+      s_base[i] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+    for (int i = threadIdx.x; i < kTreeWarps * R; i += blockDim.x) s_wc[i] = 0;
+    __syncthreads();
+    int j = c0 + threadIdx.x;
+    bool valid = j < n;
+    int x = valid ? in[j] : 0;
+    int v = valid ? dig(x) : R + (int)lane;
+    unsigned peers = __match_any_sync(0xffffffffu, v);
+    int rank = __popc(peers & lanemask_lt());
+    if (valid && rank == 0) s_wc[warp * R + v] = __popc(peers);
+    __syncthreads();
+    for (int u = threadIdx.x; u < R; u += blockDim.x) {
+      int run = 0;
+      for (int w = 0; w < kTreeWarps; ++w) {
+        int t = s_wc[w * R + u];
+        s_wc[w * R + u] = run;
+        run += t;
+      }
+      s_tot[u] = run;
+    }
+    __syncthreads();
+    if (valid) out[s_base[v] + s_wc[warp * R + v] + rank] = x;
+    __syncthreads();
+    for (int u = threadIdx.x; u < R; u += blockDim.x) s_base[u] += s_tot[u];
+    __syncthreads();
+  }
+}
+
+struct TreeShared {
+  int cnt[256];
+  int sf[256];
+  int runs[256][2];
+  int nruns;
+  int lam[kMaxDims];
+  int nlam;
+  int sh[32];
+  int base[256];
+  int tot[256];
+  int wc[kTreeWarps * 256];
+  long long off;
+  long long goff;
+  int gcount;
+  int gwrite;
+};
+
+// compare the cells of points a and b on the first L remaining dims
+__device__ __forceinline__ int cmp_prefix(const uint8_t* cc, int d, const int* lam, int a, int b, int L) {
+  for (int t = 0; t < L; ++t) {
+    int x = cc[(size_t)a * d + lam[t]], y = cc[(size_t)b * d + lam[t]];
+    if (x != y) return x < y ? -1 : 1;
+  }
+  return 0;
+}
+
+// [lo, hi) of the points of A (leaf order) sharing i's first L remaining cells
+__device__ __forceinline__ void prefix_range(const uint8_t* cc, int d, const int* lam, const int* A, int m, int i,
+                                             int L, int& lo, int& hi) {
+  int a = 0, b = m;
+  while (a < b) {
+    int mid = (a + b) >> 1;
+    if (cmp_prefix(cc, d, lam, A[mid], i, L) < 0)
+      a = mid + 1;
+    else
+      b = mid;
+  }
+  lo = a;
+  b = m;
+  while (a < b) {
+    int mid = (a + b) >> 1;
+    if (cmp_prefix(cc, d, lam, A[mid], i, L) <= 0)
+      a = mid + 1;
+    else
+      b = mid;
+  }
+  hi = a;
+}
+
+__global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
+  __shared__ TreeShared s;
+  const int w = blockIdx.x;
+  if (w >= a.nwork) return;
+  // locate the call of this work item
+  int lo = 0, hi = a.ncalls - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.work_off[mid] <= w)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int ci = lo;
+  const CallDesc C = a.calls[ci];
+  const int D = C.f + (int)(w - a.work_off[ci]);
+  const int d = a.d;
+  const int* P = a.pts_in + C.pts_off;
+  const int np = C.npts;
+  const int2* Gh = a.ghosts_in + C.ghost_off;
+  const int ng = C.nghost;
+  const uint64_t smask = C.rmask | (1ull << D);
+  const SubDesc& S = a.subs[C.child_sub + (D - C.f)];
+  const unsigned* wd = a.bitmaps + S.bitmap_off;
+  int* A = a.scratch + a.work_scratch[w];
+  int* B = A + np;
+  int* SV = B + np;  // np + 1 survivor prefix counts
+  RegionRec* rec = a.recs + (long long)w * a.cells;
+
+  // 1. cell counts and s-connection flags on D
+  for (int i = threadIdx.x; i < a.cells; i += blockDim.x) {
+    s.cnt[i] = 0;
+    s.sf[i] = 0;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < np; j += blockDim.x) {
+    int x = P[j];
+    int c = a.cc[(size_t)x * d + D];
+    atomicAdd(&s.cnt[c], 1);
+    if ((a.gz[x] >> D) & 1ull) s.sf[c] = 1;
+  }
+  for (int j = threadIdx.x; j < ng; j += blockDim.x) {
+    int2 g = Gh[j];
+    if (g.y == D) s.sf[a.cc[(size_t)g.x * d + D]] = 1;
+  }
+  __syncthreads();
+  // 2. merge runs (InscyNodeCpu.cu:179-192 with mergeWithNeighbors) and the
+  //    remaining dims of the restricted tree
+  if (threadIdx.x == 0) {
+    int nr = 0, c = 0;
+    while (c < a.cells) {
+      int c0 = c;
+      while (s.sf[c] && c < a.cells - 1) ++c;
+      s.runs[nr][0] = c0;
+      s.runs[nr][1] = c;
+      ++nr;
+      ++c;
+    }
+    s.nruns = nr;
+    int nl = 0;
+    for (int k = 0; k < d; ++k)
+      if (!((smask >> k) & 1ull)) s.lam[nl++] = k;
+    s.nlam = nl;
+  }
+  __syncthreads();
+  const int nruns = s.nruns;
+  const int nlam = s.nlam;
+  const bool last_dim = (C.nrestricted + 1 == d);
+  uint64_t lammask = ~smask;
+  if (d < 64) lammask &= (1ull << d) - 1;
+
+  for (int r = 0; r < nruns; ++r) {
+    const int c0 = s.runs[r][0], c1 = s.runs[r][1];
+    const bool drop = last_dim && c1 > c0 && s.cnt[c0] == 0;
+    // 3. restrict (+ merge): points of the run, in the parent's order
+    int m = 0;
+    if (!drop)
+      m = block_filter(
+          P, np,
+          [&](int x) {
+            int c = a.cc[(size_t)x * d + D];
+            return c >= c0 && c <= c1;
+          },
+          A, s.sh);
+    __syncthreads();
+    // 4. merged runs: stable re-sort into (remaining cells, cell on D) order
+    int* cur = A;
+    if (c1 > c0 && m > 1) {
+      int* oth = B;
+      block_sort_pass(
+          cur, oth, m, [&](int x) { return (int)a.cc[(size_t)x * d + D]; }, a.cells, s.base, s.tot, s.wc);
+      int* t = cur;
+      cur = oth;
+      oth = t;
+      for (int l = nlam - 1; l >= 0; --l) {
+        const int k = s.lam[l];
+        block_sort_pass(
+            cur, oth, m, [&](int x) { return (int)a.cc[(size_t)x * d + k]; }, a.cells, s.base, s.tot, s.wc);
+        t = cur;
+        cur = oth;
+        oth = t;
+      }
+    }
+    // 5. prune: weak density of the subspace, survivor prefix counts
+    int npp = 0;
+    for (int c = 0; c < m; c += blockDim.x) {
+      int j = c + threadIdx.x;
+      int f = 0;
+      if (j < m) {
+        int x = cur[j];
+        f = (wd[x >> 5] >> (x & 31)) & 1u;
+      }
+      int tot;
+      int inc = block_inclusive_scan<int>(f, s.sh, &tot);
+      if (j < m) SV[j] = npp + inc - f;
+      npp += tot;
+    }
+    if (threadIdx.x == 0) SV[m] = npp;
+    __syncthreads();
+    const bool passed = npp >= a.min_size;
+    long long pts_off = -1, ghost_off = -1;
+    int nghost = 0;
+    if (passed) {
+      if (threadIdx.x == 0) {
+        unsigned long long o = atomicAdd(a.out_pts_top, (unsigned long long)npp);
+        if ((long long)(o + npp) > a.out_pts_cap) {
+          atomicExch(a.err, 1);
+          s.off = -1;
+        } else {
+          s.off = (long long)o;
+        }
+      }
+      __syncthreads();
+      pts_off = s.off;
+      if (pts_off >= 0) {
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+          int x = cur[j];
+          if (SV[j + 1] != SV[j]) a.out_pts[pts_off + SV[j]] = x;
+        }
+      }
+      // 6. ghosts of the pruned tree
+      for (int phase = 0; phase < 2; ++phase) {
+        if (threadIdx.x == 0) {
+          if (phase == 0) s.gcount = 0;
+          s.gwrite = 0;
+        }
+        __syncthreads();
+        // (a) ghosts of points that were pruned here: the chain survives when a
+        //     kept point shares the cells of every remaining dim up to the chain's
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+          if (SV[j + 1] != SV[j]) continue;
+          int x = cur[j];
+          unsigned long long gb = a.gz[x] & lammask;
+          while (gb) {
+            int g = __ffsll((long long)gb) - 1;
+            gb &= gb - 1;
+            int l = __popcll(lammask & ((1ull << g) - 1));
+            int plo, phi;
+            prefix_range(a.cc, d, s.lam, cur, m, x, l + 1, plo, phi);
+            if (SV[phi] - SV[plo] > 0) {
+              if (phase == 0)
+                atomicAdd(&s.gcount, 1);
+              else {
+                int o = atomicAdd(&s.gwrite, 1);
+                if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(x, g);
+              }
+            }
+          }
+        }
+        // (b) ghosts detached earlier
+        for (int j = threadIdx.x; j < ng; j += blockDim.x) {
+          int2 gg = Gh[j];
+          int x = gg.x, g = gg.y;
+          if (g == D || g < 0 || g >= d || !((lammask >> g) & 1ull)) continue;
+          int cx = a.cc[(size_t)x * d + D];
+          if (cx < c0 || cx > c1 || drop) continue;
+          int l = __popcll(lammask & ((1ull << g) - 1));
+          int plo, phi;
+          bool alive = true;
+          if (l > 0) {
+            prefix_range(a.cc, d, s.lam, cur, m, x, l, plo, phi);
+            alive = SV[phi] - SV[plo] > 0;
+          }
+          if (!alive) continue;
+          prefix_range(a.cc, d, s.lam, cur, m, x, l + 1, plo, phi);
+          bool keep;
+          if (SV[phi] - SV[plo] > 0)
+            keep = true;  // the sibling node keeps points
+          else if (phi > plo)
+            keep = false;  // the sibling node existed and is erased with it
+          else {
+            // the sibling node exists only if a deeper detached chain passes it
+            keep = true;
+            for (int t = 0; t < ng; ++t) {
+              int2 h = Gh[t];
+              if (h.y == D || h.y < 0 || h.y >= d || !((lammask >> h.y) & 1ull)) continue;
+              int ch = a.cc[(size_t)h.x * d + D];
+              if (ch < c0 || ch > c1) continue;
+              int lh = __popcll(lammask & ((1ull << h.y) - 1));
+              if (lh > l && cmp_prefix(a.cc, d, s.lam, h.x, x, l + 1) == 0) {
+                keep = false;
+                break;
+              }
+            }
+          }
+          if (keep) {
+            if (phase == 0)
+              atomicAdd(&s.gcount, 1);
+            else {
+              int o = atomicAdd(&s.gwrite, 1);
+              if (o < s.gcount) a.out_ghosts[s.goff + o] = gg;
+            }
+          }
+        }
+        __syncthreads();
+        if (phase == 0) {
+          if (threadIdx.x == 0) {
+            unsigned long long o = atomicAdd(a.out_ghost_top, (unsigned long long)s.gcount);
+            if ((long long)(o + s.gcount) > a.out_ghost_cap) {
+              atomicExch(a.err, 2);
+              s.gcount = 0;  // nothing is written; the host retries with more room
+              o = 0;
+            }
+            s.goff = (long long)o;
+          }
+          __syncthreads();
+          if (s.gcount == 0) break;
+        }
+      }
+      ghost_off = s.goff;
+      nghost = s.gcount;
+    }
+    if (threadIdx.x == 0) {
+      RegionRec R;
+      R.call = ci;
+      R.dim = D;
+      R.c0 = c0;
+      R.c1 = c1;
+      R.npts = npp;
+      R.passed = passed ? 1 : 0;
+      R.pts_off = pts_off;
+      R.ghost_off = ghost_off;
+      R.nghost = nghost;
+      R.pad = 0;
+      rec[r] = R;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.nrecs[w] = nruns;
+}
+
+void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
+  if (L.nwork <= 0) return;
+  TreeArgs a;
+  a.calls = L.calls;
+  a.ncalls = L.ncalls;
+  a.work_off = L.work_off;
+  a.nwork = L.nwork;
+  a.pts_in = L.pts_in;
+  a.ghosts_in = L.ghosts_in;
+  a.cc = L.cc;
+  a.gz = L.gz;
+  a.n = L.n;
+  a.d = L.d;
+  a.cells = L.cells;
+  a.min_size = L.min_size;
+  a.subs = L.subs;
+  a.bitmaps = L.bitmaps;
+  a.scratch = L.scratch;
+  a.work_scratch = L.work_scratch;
+  a.recs = L.recs;
+  a.nrecs = L.nrecs;
+  a.out_pts = L.out_pts;
+  a.out_pts_top = L.out_pts_top;
+  a.out_pts_cap = L.out_pts_cap;
+  a.out_ghosts = L.out_ghosts;
+  a.out_ghost_top = L.out_ghost_top;
+  a.out_ghost_cap = L.out_ghost_cap;
+  a.err = L.err;
+  k_tree_level<<<L.nwork, kTreeThreads, 0, s>>>(a);
+}
+
+}  // namespace inscy

@@ -1,0 +1,114 @@
+/*
+ * inscy_gb300.h -- C ABI of the GB300 INSCY engine (libinscy_gb300.so).
+ *
+ * Drop-in for the GPU run of mrjakobdk/GPU_INSCY: the entry points below
+ * replace the torch-extension functions
+ *   run_gpu_5(X, neighborhood_size, F, num_obj, min_size, r, number_of_cells,
+ *             rectangular, entropy_order)          inscy_map.cpp:1070-1158
+ *   run_gpu_4(...same...)                          inscy_map.cpp:979-1067
+ * reached from GPU5() / GPU() in python/inscy.py:189-197, and return the same
+ * [subspaces, clusterings] content: one entry per clustered subspace (dims in
+ * ascending order), entries ordered as the reference's result map
+ * (vec_cmp, util.cu:633-653), each with one int32 label per point
+ * (cluster ids >= 1, -1 noise, -2 border points) -- bit-identical to the
+ * reference CPU INSCY (run_cpu3_weak, inscy_map.cpp:230-270).
+ *
+ * Plain pointers and sizes only.  Every function returns INSCY_OK (0) or an
+ * error code; inscy_last_error() then describes the failure (thread-local).
+ * Nothing calls exit(): where the reference aborts through gpuAssert
+ * (InscyArrayGpuMulti2.cu:19-29) these return INSCY_ERR_CUDA.
+ */
+#ifndef INSCY_GB300_H
+#define INSCY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  INSCY_OK = 0,
+  INSCY_ERR_ARG = 1,         /* bad argument (null pointer, n < 0, d out of range, values outside [0,1]) */
+  INSCY_ERR_CUDA = 2,        /* a CUDA call failed (no device, out of memory, launch failure) */
+  INSCY_ERR_UNSUPPORTED = 3, /* option not implemented (entropy_order != 0) */
+  INSCY_ERR_LIMIT = 4,       /* input beyond a documented limit (d > 64, ceil(1/eps) > 256, cells > 255) */
+  INSCY_ERR_INTERNAL = 5     /* a device-side consistency check failed */
+};
+
+/* Parameters of run_gpu_5 / run_cpu3_weak, same meaning and types. */
+typedef struct inscy_params {
+  float neighborhood_size; /* eps of the epsilon-neighbourhood */
+  float F;                 /* density factor */
+  int num_obj;             /* minimum number of objects term of the threshold */
+  int min_size;            /* absolute minimum cluster/region size */
+  float r;                 /* redundancy factor */
+  int number_of_cells;     /* grid cells per dimension of the SCY-tree */
+  int rectangular;         /* 0: phi density (ClusteringCpu.cu:166-176); 1: neighbour count (:178-183) */
+  int entropy_order;       /* dim order of the tree (inscy_map.cpp:61-121); only 0 is supported */
+} inscy_params;
+
+/* Execution form.  PLAIN: one level of the subspace lattice at a time, with
+ * per-level kernels.  BATCHED: the same result through the batched path (all
+ * datasets of an inscy_run_batch call share each level's launches). */
+enum { INSCY_MODE_PLAIN = 0, INSCY_MODE_BATCHED = 1 };
+
+typedef struct inscy_result inscy_result;
+
+/* Run statistics of the last run that produced a result. */
+typedef struct inscy_stats {
+  double ms_total;          /* wall time of the run (host clock) */
+  double ms_setup;          /* grid cells, trie order, candidate lists */
+  double ms_density;        /* density kernels (pass 1 + pass 2), device time */
+  double ms_density_pass1;  /* density pass 1 alone, device time */
+  double ms_tree;           /* restrict/merge/prune kernels, device time */
+  double ms_cluster;        /* union-find + component kernels, device time */
+  double ms_replay;         /* host commit (pruneRedundancy, numbering, join) */
+  double density_bytes;     /* algorithmic bytes of the density pass-1 launches */
+  double tree_bytes;        /* algorithmic bytes of the tree launches */
+  long long density_launches_pass1;
+  long long kernel_launches; /* kernels launched by this run */
+  long long calls;           /* INSCY recursion nodes */
+  long long regions;         /* restricted (and merged) regions */
+  long long subspaces;       /* subspaces evaluated */
+  long long candidates;      /* candidate pairs tested */
+  long long levels;
+  long long h2d_bytes, d2h_bytes;
+} inscy_stats;
+
+/* Replaces run_gpu_5 / run_gpu_4 (inscy_map.cpp:1070-1158 / :979-1067).
+ * X: host, float32, row-major [n, d], values in [0, 1] (the reference's
+ * cell rule, ScyTreeNode.cu:100-102, assumes this).  X is only read.  The
+ * result is owned by the caller and released with inscy_result_free. */
+int inscy_run(const float* X, int64_t n, int d, const inscy_params* p, int mode, inscy_result** out);
+
+/* Same, with X already in device memory (a CUDA device pointer) and the work
+ * queued on `stream` (a cudaStream_t, NULL = legacy default stream).  The
+ * call is synchronous: it returns once the result is on the host. */
+int inscy_run_device(const float* X_dev, int64_t n, int d, const inscy_params* p, int mode, void* stream,
+                     inscy_result** out);
+
+/* Many independent datasets (the batched workload): outs[i] receives the
+ * result of Xs[i] ([ns[i], ds[i]], host).  Same semantics as `count` calls of
+ * inscy_run. */
+int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, int count, const inscy_params* p,
+                    int mode, inscy_result** outs);
+
+/* Result access. */
+int inscy_result_count(const inscy_result* r);              /* number of clustered subspaces */
+int64_t inscy_result_n(const inscy_result* r);              /* number of points */
+int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap); /* returns |S|, writes min(|S|,cap) dims */
+int inscy_result_labels(const inscy_result* r, int i, int32_t* out);        /* copies n labels */
+int inscy_result_stats(const inscy_result* r, inscy_stats* out);
+void inscy_result_free(inscy_result* r);
+
+/* Description of the last error of the calling thread ("" if none). */
+const char* inscy_last_error(void);
+
+/* Library version string. */
+const char* inscy_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* INSCY_GB300_H */

@@ -1,0 +1,87 @@
+"""The C-ABI library: it builds, loads, exports what include/inscy_gb300.h
+declares, and rejects bad arguments with an error code (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from gpu_inscy_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "inscy_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(inscy_[a-z_]+)\s*\(", src)))
+
+
+def test_header_lists_the_python_exports():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(engine):
+    for name in declared_functions():
+        assert hasattr(engine, name), name
+
+
+def test_version(engine):
+    assert engine.inscy_version().decode().startswith("inscy_gb300")
+
+
+def _call(engine, X, **kw):
+    p = _lib.make_params(**{**dict(neighborhood_size=0.1, F=1.0, num_obj=2, min_size=4, r=1.0,
+                                   number_of_cells=4), **kw})
+    h = ctypes.c_void_p()
+    X = np.ascontiguousarray(X, np.float32)
+    rc = engine.inscy_run(X.ctypes.data if X.size else None, X.shape[0], X.shape[1] if X.ndim == 2 else 0,
+                          ctypes.byref(p), 0, ctypes.byref(h))
+    return rc, h
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(neighborhood_size=0.0), _lib.INSCY_ERR_ARG),
+    (dict(number_of_cells=0), _lib.INSCY_ERR_ARG),
+    (dict(number_of_cells=300), _lib.INSCY_ERR_LIMIT),
+    (dict(entropy_order=1), _lib.INSCY_ERR_UNSUPPORTED),
+])
+def test_bad_parameters_are_rejected(engine, kw, code):
+    rc, h = _call(engine, np.random.default_rng(0).random((10, 3)), **kw)
+    assert rc == code
+    assert engine.inscy_last_error().decode()
+
+
+def test_too_many_dims(engine):
+    rc, _ = _call(engine, np.random.default_rng(0).random((4, 65)))
+    assert rc == _lib.INSCY_ERR_LIMIT
+
+
+def test_values_outside_unit_interval(engine):
+    X = np.random.default_rng(0).random((10, 3)).astype(np.float32)
+    X[3, 1] = 1.5
+    rc, _ = _call(engine, X)
+    assert rc == _lib.INSCY_ERR_ARG
+    X[3, 1] = np.nan
+    rc, _ = _call(engine, X)
+    assert rc == _lib.INSCY_ERR_ARG
+
+
+def test_null_output_pointer(engine):
+    p = _lib.make_params(0.1, 1.0, 2, 4, 1.0, 4)
+    X = np.zeros((2, 2), np.float32)
+    assert engine.inscy_run(X.ctypes.data, 2, 2, ctypes.byref(p), 0, None) == _lib.INSCY_ERR_ARG
+
+
+def test_result_accessors_tolerate_null(engine):
+    assert engine.inscy_result_count(None) == 0
+    assert engine.inscy_result_n(None) == 0
+    engine.inscy_result_free(None)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(ImportError):
+        _lib.load()

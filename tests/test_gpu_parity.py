@@ -1,0 +1,156 @@
+"""CUDA engine vs the reference CPU INSCY: labels, subspaces and cluster
+counts must be bit-identical.
+
+* against the reference's own outputs (golden fixtures);
+* against the oracle on seeded inputs the oracle finishes in seconds;
+* edge cases (empty, single point, one dim, duplicates, tiny/huge min_size).
+All calls go through the C ABI (libinscy_gb300.so).
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from golden_io import assert_same, family_cases, small_case
+from gpu_inscy_gb300 import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_run(X, mode=_lib.MODE_PLAIN, **p):
+    subs, labels, stats = _lib.run_host(X, _lib.make_params(**p), mode)
+    return (subs, labels), stats
+
+
+@pytest.mark.parametrize("rect", [0, 1])
+def test_small_workload_matches_reference_outputs(engine, rect):
+    X, p, want = small_case(rect)
+    got, stats = gpu_run(X, **p)
+    assert_same(got, want, "small rect=%d" % rect)
+    assert stats["calls"] > 0 and stats["kernel_launches"] > 0
+
+
+@pytest.mark.parametrize("case", [c for c in family_cases() if c[2]["entropy_order"] == 0],
+                         ids=lambda c: "family%d" % c[0])
+def test_family_matches_reference_outputs(engine, case):
+    i, X, p, want = case
+    got, _ = gpu_run(X, **p)
+    assert_same(got, want, "family %d" % i)
+
+
+def _random_case(seed):
+    rng = np.random.default_rng(424242 + seed)
+    n = int(rng.integers(50, 2500))
+    d = int(rng.integers(1, 8))
+    X = synth.make_random(seed, n, d, n_clusters=int(rng.integers(1, 6)), std=float(rng.uniform(0.01, 0.08)))
+    p = dict(neighborhood_size=float(rng.choice([0.02, 0.03, 0.05, 0.08, 0.12, 0.2])), F=1.0,
+             num_obj=int(rng.integers(1, 8)), min_size=int(rng.integers(1, 40)),
+             r=float(rng.choice([0.6, 1.0, 1.4])), number_of_cells=int(rng.integers(2, 8)),
+             rectangular=bool(rng.integers(0, 2)))
+    return X, p
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_cases_match_oracle(engine, seed):
+    X, p = _random_case(seed)
+    got, _ = gpu_run(X, **p)
+    assert_same(got, orc.run(X, **p), "seed %d" % seed)
+
+
+def test_plain_workload_shape_matches_oracle(engine):
+    # the 25,000 x 15 workload's generator at a size the oracle finishes fast
+    X = synth.make_plain(3, n=4000, d=10)
+    p = synth.PARAMS["plain"]
+    got, stats = gpu_run(X, **p)
+    want = orc.run(X, **p)
+    assert_same(got, want, "plain-shaped")
+    assert len(want[0]) > 0
+
+
+def test_batched_mode_equals_plain(engine):
+    X, p = _random_case(101)
+    a, _ = gpu_run(X, mode=_lib.MODE_PLAIN, **p)
+    b, _ = gpu_run(X, mode=_lib.MODE_BATCHED, **p)
+    assert_same(a, b, "modes")
+
+
+def test_device_pointer_entry_equals_host_entry(engine):
+    torch = pytest.importorskip("torch")
+    X, p = _random_case(7)
+    want, _ = gpu_run(X, **p)
+    Xd = torch.from_numpy(X).cuda()
+    subs, labels, _ = _lib.run_device(Xd.data_ptr(), X.shape[0], X.shape[1], _lib.make_params(**p),
+                                      torch.cuda.current_stream().cuda_stream)
+    assert_same((subs, labels), want, "device entry")
+
+
+def test_drop_in_api_returns_reference_types(engine):
+    from gpu_inscy_gb300 import GPU, GPU5, count_number_of_clusters
+    torch = pytest.importorskip("torch")
+    X, p = _random_case(3)
+    subs, clus = GPU(torch.from_numpy(X), **p)
+    assert isinstance(subs, list) and isinstance(clus, list)
+    assert all(isinstance(v, int) for s in subs for v in s)
+    want = orc.run(X, **p)
+    assert_same((subs, clus), want, "GPU()")
+    assert count_number_of_clusters(subs, clus) == count_number_of_clusters(*want)
+    subs5, clus5 = GPU5(torch.from_numpy(X).cuda(), **p)
+    assert_same((subs5, clus5), want, "GPU5() with a device tensor")
+
+
+def test_batch_entry(engine):
+    cases = [_random_case(s) for s in (11, 12, 13)]
+    p = cases[0][1]
+    res = _lib.run_batch([c[0] for c in cases], _lib.make_params(**p))
+    for (X, _), (subs, labels, _) in zip(cases, res):
+        assert_same((subs, labels), orc.run(X, **p), "batch")
+
+
+# ---------------------------------------------------------------- edge cases
+BASE = dict(neighborhood_size=0.1, F=1.0, num_obj=2, min_size=3, r=1.0, number_of_cells=4)
+
+
+def test_empty_input(engine):
+    (subs, labels), _ = gpu_run(np.zeros((0, 4), np.float32), **BASE)
+    assert subs == [] and labels.shape[0] == 0
+
+
+def test_single_point(engine):
+    X = np.array([[0.5, 0.5]], np.float32)
+    got, _ = gpu_run(X, **{**BASE, "min_size": 0})
+    assert_same(got, orc.run(X, **{**BASE, "min_size": 0}), "single point")
+
+
+@pytest.mark.parametrize("min_size", [0, 1, 10**6])
+def test_min_size_extremes(engine, min_size):
+    X, p = _random_case(5)
+    p["min_size"] = min_size
+    got, _ = gpu_run(X, **p)
+    assert_same(got, orc.run(X, **p), "min_size=%d" % min_size)
+
+
+def test_one_dimension(engine):
+    X = synth.make_random(9, 700, 1, n_clusters=3, std=0.02)
+    got, _ = gpu_run(X, **BASE)
+    assert_same(got, orc.run(X, **BASE), "d=1")
+
+
+def test_duplicate_points_and_cell_edges(engine):
+    rng = np.random.default_rng(1)
+    base = rng.random((40, 3)).astype(np.float32)
+    X = np.concatenate([base, base, np.round(base * 4) / 4]).clip(0, 1).astype(np.float32)
+    X[:5] = 1.0
+    X[5:10] = 0.0
+    for rect in (False, True):
+        p = {**BASE, "rectangular": rect, "neighborhood_size": 0.2}
+        got, _ = gpu_run(X, **p)
+        assert_same(got, orc.run(X, **p), "duplicates rect=%s" % rect)
+
+
+def test_wide_neighbourhood_many_s_connections(engine):
+    # large eps relative to the cell width: every cell is s-connected and
+    # most pruned points leave detached s-connection chains behind
+    for seed in range(4):
+        X = synth.make_random(seed, 300, 4, n_clusters=3, std=0.05)
+        p = dict(neighborhood_size=0.3, F=1.0, num_obj=6, min_size=5, r=1.0, number_of_cells=6)
+        got, _ = gpu_run(X, **p)
+        assert_same(got, orc.run(X, **p), "wide eps seed %d" % seed)
