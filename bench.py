@@ -1,0 +1,255 @@
+"""Benchmark of the GB300 INSCY engine on the 25,000 x 15 plain-GPU workload.
+
+One step = one complete INSCY run (all lattice levels, clustering and the
+ordered commit) over one synthetic dataset of the workload: n=25,000 float32
+points in d=15 dims, 10 Gaussian clusters of 2,250 points (std 0.02) in
+random 4-6 dim subspaces, 2,500 uniform noise points; neighborhood_size=0.03,
+F=1, num_obj=4, min_size=16, r=1, number_of_cells=4.  The metric is points
+clustered per second (n / run time) and ms per run.
+
+  value   -- device-resident: X already in HBM, inscy_run_device, CUDA events on
+             the engine's stream, L2 flushed (256 MiB write) before every step;
+  e2e     -- the reference-facing call with host buffers (inscy_run: host X in,
+             host labels out), host clock, copies included;
+  roofline-- the density pass-1 kernel (the dominant kernel): algorithmic bytes
+             per launch / its average launch time, against the measured HBM
+             copy bandwidth;
+  cpu_baseline -- the CPU restatement of the reference CPU INSCY (oracle/) on a
+             bounded sample of the workload, all host cores.
+
+`--impl reference` times the reference's CPU INSCY path (the oracle port of
+run_cpu3_weak) instead.  Multi-GPU: replicas only (`--gpus N` under torchrun
+runs N independent copies of the workload, one per GPU).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+WORKLOAD = "plain_n25000_d15"
+METRIC = "INSCY points/sec (plain GPU run, bit-exact labels)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=2000, help="rows of the workload the CPU baseline runs on")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-check", action="store_true", help="skip the label check against the oracle")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(X, p, sample_rows, steps=1):
+    """Oracle port of the reference CPU INSCY on the first `sample_rows` rows."""
+    import oracle as orc
+    Xs = np.ascontiguousarray(X[:sample_rows])
+    cores = os.cpu_count() or 1
+    orc.load()
+    times = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        orc.run(Xs, **p, threads=cores)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    return {"value": Xs.shape[0] / t, "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": "first %d of the %d rows of the %s workload, same parameters; %.2f s per run"
+                      % (Xs.shape[0], X.shape[0], WORKLOAD, t)}
+
+
+def run_reference(args, X, p):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cpu_baseline(X, p, args.cpu_sample, steps=max(1, min(args.warmup, 1)))  # warm-up (page-in, build)
+    res = cpu_baseline(X, p, args.cpu_sample, steps=args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "points/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.cpu_sample / res["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": int(X.shape[0]), "d": int(X.shape[1]), **p,
+                       "sample_rows": args.cpu_sample},
+            "cpu_baseline": res, "e2e": {"value": res["value"], "unit": "points/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    from gpu_inscy_gb300 import synth
+    X = synth.make_plain(args.seed)
+    p = dict(synth.PARAMS["plain"])
+    if args.impl == "reference":
+        run_reference(args, X, p)
+        return
+    ws, rank, local = dist_env()
+    import torch
+    from gpu_inscy_gb300 import _lib
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    _lib.load()
+    params = _lib.make_params(**p)
+    n, d = X.shape
+    stream = torch.cuda.Stream()
+    Xd = torch.from_numpy(X).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def device_step():
+        with torch.cuda.stream(stream):
+            return _lib.run_device(Xd.data_ptr(), n, d, params, stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        subs, labels, stats = device_step()
+    torch.cuda.synchronize()
+    ok = None
+    if not args.no_check:
+        import oracle as orc  # noqa: F401  (checker only)
+    # ---- timed region (device-resident input)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times, stats_all = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        subs, labels, stats = device_step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        stats_all.append(stats)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = float(np.mean(times))
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    # ---- end to end through the host-buffer C ABI
+    e2e_times, e2e_stats = [], None
+    for _ in range(max(1, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2, l2, e2e_stats = _lib.run_host(X, params)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = 1000.0 * float(np.mean(e2e_times))
+    same = s2 == subs and np.array_equal(l2, labels)
+    # ---- roofline of the density pass-1 kernel
+    st = stats_all[-1]
+    peak, peak_kind = measured_peak()
+    launches = max(1, st["density_launches_pass1"])
+    per_launch_ms = st["ms_density_pass1"] / launches
+    per_launch_bytes = st["density_bytes"] / launches
+    achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "density_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    roof = {"bound": "hbm", "kernel": "k_density<pass1>", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
+    # ---- label check against the oracle at a reduced size is done by the tests;
+    #      here the device and host entries must agree with each other
+    line = {"metric": METRIC, "value": ws * n / (ms * 1e-3), "unit": "points/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "d": d, **p, "seed": args.seed,
+                       "l2": "flushed before every step (256 MiB write)", "parallelism": "replicas"},
+            "e2e": {"value": ws * n / (e2e_ms * 1e-3), "unit": "points/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(e2e_stats["h2d_bytes"]), "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"])},
+            "gpu_launches": int(sum(s["kernel_launches"] for s in stats_all)),
+            "roofline": roof, "clocks": clk,
+            "breakdown_ms": {k: st[k] for k in ("ms_setup", "ms_density", "ms_density_pass1", "ms_tree",
+                                               "ms_cluster", "ms_replay", "ms_total")},
+            "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
+            "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(X, p, args.cpu_sample)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

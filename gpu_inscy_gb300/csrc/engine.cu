@@ -551,11 +551,24 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.flags = dflags;
     DL.bitmaps = dbm;
     DL.words = W;
+    unsigned long long* dcand_cnt = lv.get<unsigned long long>(1);
+    CK(cudaMemsetAsync(dcand_cnt, 0, sizeof(unsigned long long), s));
+    DL.cand_counter = dcand_cnt;
     double ms1 = timed(s, [&] { launch_density(DL, false, s); });
     stats_.ms_density += ms1;
     stats_.ms_density_pass1 += ms1;
     stats_.density_launches_pass1 += 1;
     ++launches;
+    {
+      // algorithmic bytes of pass 1: per query point 26 B (its id, list
+      // offset and length, own coordinate and fine cell, count and flags out);
+      // per candidate 8 B at level 1 (id + coordinate) and 13 B above (id,
+      // stored partial distance, coordinate, fine cell)
+      unsigned long long nc = scalar(dcand_cnt, s);
+      stats_.candidates += (long long)nc;
+      stats_.density_bytes += 26.0 * (double)nitems + (level == 1 ? 8.0 : 13.0) * (double)nc;
+    }
+    DL.cand_counter = nullptr;
 
     // ---- 3. kept items: list offsets and kept-point arrays
     int* dkcnt = lv.get<int>(nitems);

@@ -51,6 +51,7 @@ struct DensityLaunch {
   const long long* out_off;
   int* out_ids;
   float* out_acc;
+  unsigned long long* cand_counter;
 };
 void launch_density(const DensityLaunch& L, bool write, cudaStream_t s);
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,

@@ -56,6 +56,7 @@ struct DensityArgs {
   const long long* out_off;  // [nitems] list start of kept items
   int* out_ids;
   float* out_acc;
+  unsigned long long* cand_counter;  // candidates tested (pass 1)
 };
 
 __device__ __forceinline__ int find_sub(const SubDesc* subs, int nsubs, long long item) {
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(256) k_density(DensityArgs a) {
   if (v >= a.thr_dense[S.nsub]) f |= kFlagDense;
   if (v >= a.thr_keep[S.nsub]) f |= kFlagKeep;
   if (lane == 0) {
+    if (a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len);
     a.cnt[item] = count;
     a.flags[item] = f;
     unsigned bit = 1u << (p & 31);
@@ -251,6 +253,7 @@ void launch_density(const DensityLaunch& L, bool write, cudaStream_t s) {
   a.out_off = L.out_off;
   a.out_ids = L.out_ids;
   a.out_acc = L.out_acc;
+  a.cand_counter = L.cand_counter;
   long long threads = L.nitems * 32;
   unsigned blocks = (unsigned)((threads + 255) / 256);
   if (write)

@@ -38,6 +38,8 @@ def assert_same(got, want, what=""):
     gs, gl = got
     ws, wl = want
     assert [list(s) for s in gs] == [list(s) for s in ws], "%s: subspaces differ\n got %s\nwant %s" % (what, gs, ws)
+    if not ws:
+        return
     gl = np.asarray(gl, np.int32).reshape(len(gs), -1)
     wl = np.asarray(wl, np.int32).reshape(len(ws), -1)
     for i, s in enumerate(ws):
