@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -211,11 +212,16 @@ struct HSub {  // components of one clustered subspace
   std::vector<int> borders;
 };
 
+// One result-map entry (a clustered subspace) during the commit.
 struct Entry {
   uint64_t mask = 0;
-  std::vector<int> lab;
-  int maxv = 0;
-  std::vector<int> szp;  // size of the point's cluster (0: none)
+  std::vector<int> lab;             // one label per point (-1 noise, -2 border)
+  std::vector<int> size;            // points per label (index = label)
+  std::vector<std::vector<int>> mem;  // points ever given each label (validated lazily)
+  int maxv = -100000;               // v_max(lab) (util.cu:566-574)
+  int maxsz = 0;                    // largest cluster
+  std::vector<int> by_size;         // labels in ascending size (rebuilt when dirty)
+  bool dirty = true;
 };
 
 struct HostParams {
@@ -299,8 +305,11 @@ class Engine {
   std::vector<HCall> calls_;
   std::vector<HLevel> levels_;
   std::vector<HSub> subs_;
-  std::map<std::vector<int>, Entry, SubspaceOrder> result_;
-  std::vector<std::vector<int>> vbuf_;  // one n-vector of labels per recursion depth
+  std::vector<std::unique_ptr<Entry>> ents_;  // result map entries, in insertion order
+  std::vector<uint64_t> emask_;               // their subspaces
+  std::map<uint64_t, int> eidx_;              // subspace -> entry
+  std::vector<uint64_t> tbits_;               // region bitmap scratch
+  std::vector<std::vector<int>> vbuf_;        // one n-vector of labels per recursion depth
   inscy_stats stats_;
 };
 
@@ -315,7 +324,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   calls_.clear();
   levels_.clear();
   subs_.clear();
-  result_.clear();
+  ents_.clear();
+  emask_.clear();
+  eidx_.clear();
   out_dims.clear();
   out_labels.clear();
   if (n == 0) {
@@ -520,7 +531,28 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     SubDesc* dsubs = lv.get<SubDesc>(nsubs);
     h2d(dsubs, subs.data(), sizeof(SubDesc) * nsubs, s);
 
-    // ---- 2. density pass 1
+    // groups: the children of one parent subspace, walked child-fastest
+    std::vector<GroupDesc> groups;
+    {
+      long long wo = 0;
+      for (int i = 0; i < nsubs;) {
+        int j = i;
+        while (j < nsubs && subs[j].parent == subs[i].parent) ++j;
+        GroupDesc g;
+        g.warp_off = wo;
+        g.sub_base = i;
+        g.nchild = j - i;
+        g.nquery = subs[i].nquery;
+        g.pad = 0;
+        wo += (long long)g.nchild * g.nquery;
+        groups.push_back(g);
+        i = j;
+      }
+    }
+    GroupDesc* dgroups = lv.get<GroupDesc>(groups.size());
+    h2d(dgroups, groups.data(), sizeof(GroupDesc) * groups.size(), s);
+
+    // ---- 2. neighbour counts of every (subspace, point)
     int* dcnt = lv.get<int>(nitems);
     uint8_t* dflags = lv.get<uint8_t>(nitems);
     unsigned* dbm = keepmem->get<unsigned>((size_t)nsubs * 3 * W);
@@ -530,6 +562,8 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.subs = dsubs;
     DL.nsubs = nsubs;
     DL.nitems = nitems;
+    DL.groups = dgroups;
+    DL.ngroups = (int)groups.size();
     DL.X = dX;
     DL.fc = dfc;
     DL.n = ni;
@@ -554,45 +588,50 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     unsigned long long* dcand_cnt = lv.get<unsigned long long>(1);
     CK(cudaMemsetAsync(dcand_cnt, 0, sizeof(unsigned long long), s));
     DL.cand_counter = dcand_cnt;
-    double ms1 = timed(s, [&] { launch_density(DL, false, s); });
+    double ms1 = timed(s, [&] { launch_neighbours(DL, false, s); });
     stats_.ms_density += ms1;
     stats_.ms_density_pass1 += ms1;
     stats_.density_launches_pass1 += 1;
     ++launches;
     {
-      // algorithmic bytes of pass 1: per query point 26 B (its id, list
-      // offset and length, own coordinate and fine cell, count and flags out);
-      // per candidate 8 B at level 1 (id + coordinate) and 13 B above (id,
-      // stored partial distance, coordinate, fine cell)
+      // algorithmic bytes of the count pass: per query point 26 B (its id,
+      // list offset and length, own coordinate and fine cell, count out); per
+      // candidate 8 B at level 1 (id + coordinate) and 13 B above (id, stored
+      // partial distance, coordinate, fine cell)
       unsigned long long nc = scalar(dcand_cnt, s);
       stats_.candidates += (long long)nc;
       stats_.density_bytes += 26.0 * (double)nitems + (level == 1 ? 8.0 : 13.0) * (double)nc;
     }
     DL.cand_counter = nullptr;
 
-    // ---- 3. kept items: list offsets and kept-point arrays
-    int* dkcnt = lv.get<int>(nitems);
-    int* dkflag = lv.get<int>(nitems);
+    // ---- 3. ordered lists of every item, then densities and flags
     long long* dloff = lv.get<long long>(nitems);
-    long long* dkpos = lv.get<long long>(nitems + 1);
     long long* dtot = lv.get<long long>(2);
     void* sums = scan_sums(std::max(nitems, (long long)nsubs * W) + 1, s, lv);
+    launch_exclusive_scan_i2ll(dcnt, dloff, nitems, dtot, sums, s);
+    launches += 3;
+    const long long L = scalar(dtot, s);
+    int* lids = keepmem->get<int>(L);
+    float* lacc = keepmem->get<float>(L);
+    DL.loff = dloff;
+    DL.lids = lids;
+    DL.lacc = lacc;
+    stats_.ms_density += timed(s, [&] {
+      launch_neighbours(DL, true, s);
+      launch_density_flags(DL, s);
+    });
+    launches += 2;
+    // kept items
+    int* dkcnt = lv.get<int>(nitems);
+    int* dkflag = lv.get<int>(nitems);
+    long long* dkpos = lv.get<long long>(nitems + 1);
     launch_keep_counts(dcnt, dflags, nitems, dkcnt, dkflag, s);
-    launch_exclusive_scan_i2ll(dkcnt, dloff, nitems, dtot, sums, s);
     launch_exclusive_scan_i2ll(dkflag, dkpos, nitems, dtot + 1, sums, s);
-    launches += 7;
-    long long htot[2];
-    d2h(htot, dtot, sizeof(htot), s);
-    const long long L = htot[0], K = htot[1];
+    launches += 4;
+    const long long K = scalar(dtot + 1, s);
     int* keep_ids = keepmem->get<int>(K);
     long long* keep_loff = keepmem->get<long long>(K);
     int* keep_lcnt = keepmem->get<int>(K);
-    int* lids = keepmem->get<int>(L);
-    float* lacc = keepmem->get<float>(L);
-    DL.out_off = dloff;
-    DL.out_ids = lids;
-    DL.out_acc = lacc;
-    stats_.ms_density += timed(s, [&] { launch_density(DL, true, s); });
     launch_keep_compact(dsubs, nsubs, nitems, dflags, dcnt, dkpos, dloff, prev.keep_ids, keep_ids, keep_loff,
                         keep_lcnt, s);
     launches += 2;
@@ -606,10 +645,8 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     int* dkwr = keepmem->get<int>((size_t)nsubs * W + 1);
     {
       int* pc = lv.get<int>((size_t)nsubs * W + 1);
-      for (int i = 0; i < nsubs; ++i) {
-        launch_word_popc(dbm + (size_t)i * 3 * W + 2 * W, W, pc + (size_t)i * W, s);
-        ++launches;
-      }
+      launch_keep_popc(dbm, nsubs, W, pc, s);
+      ++launches;
       int* dt = lv.get<int>(1);
       launch_exclusive_scan_int(pc, dkwr, (long long)nsubs * W, dt, sums, s);
       launches += 3;
@@ -795,13 +832,14 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       int* is_root = lv.get<int>(K + 1);
       int* root_id = lv.get<int>(K + 1);
       int* comp = lv.get<int>(K + 1);
+      int* root_of = lv.get<int>(K + 1);
       int* dnc = lv.get<int>(1);
       long long ncomp = 0;
       std::vector<int> cbase(nsubs + 1);
       stats_.ms_cluster += timed(s, [&] {
         launch_uf_init(CA.uf, K, s);
         launch_uf_union(CA, s);
-        launch_uf_flatten(CA, is_root, s);
+        launch_uf_flatten(CA, is_root, root_of, s);
         launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
       });
       launches += 6;
@@ -829,7 +867,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       CK(cudaMemsetAsync(novf, 0, sizeof(int), s));
       long long* dmtot = lv.get<long long>(2);
       stats_.ms_cluster += timed(s, [&] {
-        launch_comp_ids(CA, root_id, comp, mcount, s);
+        launch_comp_ids(CA, root_id, root_of, comp, mcount, s);
         launch_exclusive_scan_i2ll(mcount, moff, ncomp, dmtot, sums, s);
       });
       launches += 4;
@@ -920,13 +958,21 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   // ---------------------------------------------------------------- commit
   auto t_rep0 = std::chrono::steady_clock::now();
   vbuf_.assign(d + 2, std::vector<int>());
+  tbits_.assign(((size_t)n + 63) / 64, 0);
   replay(0);
   stats_.ms_replay = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_rep0).count();
-  for (auto& e : result_) {
-    out_dims.push_back(e.first);
-    out_labels.push_back(std::move(e.second.lab));
+  {
+    // the result map's order (vec_cmp)
+    std::map<std::vector<int>, int, SubspaceOrder> order;
+    for (size_t i = 0; i < ents_.size(); ++i) order.emplace(dims_of(emask_[i]), (int)i);
+    for (auto& kv : order) {
+      out_dims.push_back(kv.first);
+      out_labels.push_back(std::move(ents_[kv.second]->lab));
+    }
   }
-  result_.clear();
+  ents_.clear();
+  emask_.clear();
+  eidx_.clear();
   stats_.kernel_launches = launches;
   stats_.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
   st = stats_;
@@ -962,22 +1008,65 @@ void Engine::replay(int ci) {
 
 // pruneRedundancy (ScyTreeNode.cu:669-734): over result entries whose
 // subspace contains S, the smallest cluster touching the region's points;
-// the largest of these must stay below |region| * r.
+// the region is clustered unless the largest of these reaches |region| * r.
+// The answer only depends on that maximum, so the scan stops as soon as it
+// is decided; per entry the smallest touched cluster is found either by
+// scanning the region's points or, for large regions, by walking the entry's
+// clusters smallest-first against a bitmap of the region.
 bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
   const int* pts = levels_[c.level].pts.data() + c.pts_off;
+  const int m = c.npts;
+  const double thr = (double)((float)m * hp_.r);
+  const bool use_bits = (long long)m * 8 > n_;
+  if (use_bits)
+    for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] |= 1ull << (pts[j] & 63);
   int max_min = 0;
-  for (auto& e : result_) {
-    const Entry& H = e.second;
-    if ((H.mask & smask) != smask) continue;
+  bool result = true;
+  const size_t ne = ents_.size();
+  for (size_t i = 0; i < ne; ++i) {
+    if ((emask_[i] & smask) != smask) continue;
+    Entry& E = *ents_[i];
     int mn = -1;
-    for (int j = 0; j < c.npts; ++j) {
-      int p = pts[j];
-      if (H.lab[p] >= 0 && (mn == -1 || H.szp[p] < mn)) mn = H.szp[p];
+    if (!use_bits) {
+      for (int j = 0; j < m; ++j) {
+        int l = E.lab[pts[j]];
+        if (l >= 0) {
+          int v = E.size[l];
+          if (mn == -1 || v < mn) mn = v;
+        }
+      }
+    } else {
+      if (E.dirty) {
+        E.by_size.clear();
+        for (int l = 0; l < (int)E.size.size(); ++l)
+          if (E.size[l] > 0) E.by_size.push_back(l);
+        std::stable_sort(E.by_size.begin(), E.by_size.end(), [&](int a, int b) { return E.size[a] < E.size[b]; });
+        E.dirty = false;
+      }
+      for (int l : E.by_size) {
+        bool hit = false;
+        for (int q : E.mem[l])
+          if (E.lab[q] == l && ((tbits_[q >> 6] >> (q & 63)) & 1ull)) {
+            hit = true;
+            break;
+          }
+        if (hit) {
+          mn = E.size[l];
+          break;
+        }
+      }
     }
-    if (mn > max_min) max_min = mn;
+    if (mn > max_min) {
+      max_min = mn;
+      if (!(thr > (double)max_min * 1.0)) {
+        result = false;
+        break;
+      }
+    }
   }
-  if (max_min == 0) return true;
-  return (double)((float)c.npts * hp_.r) > (double)max_min * 1.0;
+  if (use_bits)
+    for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] = 0;
+  return max_min == 0 ? true : result;
 }
 
 // BFS numbering of INSCYClusteringImplCPUAll (ClusteringCpu.cu:317-389):
@@ -1007,70 +1096,97 @@ void Engine::cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>&
   }
 }
 
-// join (util.cu:655-743)
+// join (util.cu:655-743): drop clusters below min_size, drop clusters a
+// superset subspace already covers with a cluster more than r times larger,
+// then insert the clustering or merge it into the subspace's entry (new
+// labels offset by the old maximum + 1, -2 marks overwrite).
 void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, uint64_t smask) {
   if (nlabels == 0) return;
   std::vector<int> sizes(nlabels + 1, 0);
   for (int p : touched)
     if (V[p] >= 0) sizes[V[p]]++;
-  bool any = false;
+  int minsz = INT32_MAX;
   for (int p : touched)
     if (V[p] >= 0) {
       if (sizes[V[p]] < hp_.min_size)
         V[p] = -1;
       else
-        any = true;
+        minsz = std::min(minsz, sizes[V[p]]);
     }
-  if (!any) return;
+  if (minsz == INT32_MAX) return;
   std::vector<char> drop(nlabels + 1, 0);
-  for (auto& e : result_) {
-    const Entry& H = e.second;
-    if ((H.mask & smask) != smask) continue;
+  const size_t ne = ents_.size();
+  for (size_t i = 0; i < ne; ++i) {
+    if ((emask_[i] & smask) != smask) continue;
+    const Entry& H = *ents_[i];
+    // nothing can be dropped when even the smallest cluster times r is not
+    // below the entry's largest cluster (float comparisons as the reference)
+    if (hp_.r >= 0.f && !((float)minsz * hp_.r < (float)H.maxsz)) continue;
     bool hit = false;
     for (int p : touched) {
       int c = V[p];
-      if (c >= 0 && H.lab[p] >= 0 && (float)sizes[c] * hp_.r < (float)H.szp[p]) {
+      if (c < 0) continue;
+      int h = H.lab[p];
+      if (h >= 0 && (float)sizes[c] * hp_.r < (float)H.size[h]) {
         drop[c] = 1;
         hit = true;
       }
     }
-    if (hit)
+    if (hit) {
       for (int p : touched)
         if (V[p] >= 0 && drop[V[p]]) V[p] = -1;
-  }
-  any = false;
-  for (int p : touched)
-    if (V[p] >= 0) any = true;
-  if (!any) return;
-  std::vector<int> key = dims_of(smask);
-  auto it = result_.find(key);
-  Entry* E;
-  if (it != result_.end()) {
-    E = &it->second;
-    const int m = E->maxv;
-    for (int p : touched) {
-      if (V[p] == -2)
-        E->lab[p] = -2;
-      else if (V[p] >= 0)
-        E->lab[p] = m + 1 + V[p];
+      minsz = INT32_MAX;
+      for (int p : touched)
+        if (V[p] >= 0) minsz = std::min(minsz, sizes[V[p]]);
+      if (minsz == INT32_MAX) return;
     }
-  } else {
-    Entry ne;
-    ne.mask = smask;
-    ne.lab.assign(n_, -1);
-    for (int p : touched) ne.lab[p] = V[p];
-    E = &result_.emplace(key, std::move(ne)).first->second;
   }
-  // refresh the entry's max label and per-point cluster sizes
-  int mx = -100000;
-  for (int v : E->lab) mx = std::max(mx, v);
+  Entry* E;
+  int off = 0;
+  auto it = eidx_.find(smask);
+  if (it != eidx_.end()) {
+    E = ents_[it->second].get();
+    off = E->maxv + 1;  // m + 1 + label
+  } else {
+    std::unique_ptr<Entry> ne(new Entry());
+    ne->mask = smask;
+    ne->lab.assign(n_, -1);
+    E = ne.get();
+    eidx_[smask] = (int)ents_.size();
+    ents_.push_back(std::move(ne));
+    emask_.push_back(smask);
+    off = 0;
+  }
+  for (int p : touched) {
+    int v = V[p];
+    if (v == -1) continue;
+    int nv = v == -2 ? -2 : off + v;
+    int ov = E->lab[p];
+    if (ov >= 0) E->size[ov]--;
+    E->lab[p] = nv;
+    if (nv >= 0) {
+      if ((int)E->size.size() <= nv) {
+        E->size.resize(nv + 1, 0);
+        E->mem.resize(nv + 1);
+      }
+      E->size[nv]++;
+      E->mem[nv].push_back(p);
+    }
+  }
+  // v_max over the whole vector: the largest label that still has points,
+  // else the largest of -1/-2 present
+  int mx = -100000, msz = 0;
+  for (int l = (int)E->size.size() - 1; l >= 0; --l)
+    if (E->size[l] > 0) {
+      if (mx == -100000) mx = l;
+      msz = std::max(msz, E->size[l]);
+    }
+  if (mx == -100000) {
+    for (int v : E->lab) mx = std::max(mx, v);
+  }
   E->maxv = mx;
-  std::vector<int> cnt(std::max(mx, 0) + 1, 0);
-  for (int v : E->lab)
-    if (v >= 0) cnt[v]++;
-  E->szp.assign(n_, 0);
-  for (long long i = 0; i < n_; ++i)
-    if (E->lab[i] >= 0) E->szp[i] = cnt[E->lab[i]];
+  E->maxsz = msz;
+  E->dirty = true;
 }
 
 }  // namespace inscy

@@ -62,6 +62,15 @@ struct SubDesc {
   long long bitmap_off; // word offset of this subspace's flag bitmaps
 };
 
+// The children of one parent subspace (contiguous subspace indices).
+struct GroupDesc {
+  long long warp_off;  // first work item (warp) of the group
+  int sub_base;
+  int nchild;
+  int nquery;
+  int pad;
+};
+
 // Per-point flag bits of a (subspace, point) evaluation.
 enum : uint8_t { kFlagWeak = 1, kFlagDense = 2, kFlagKeep = 4 };
 

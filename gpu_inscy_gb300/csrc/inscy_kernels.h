@@ -29,6 +29,8 @@ struct DensityLaunch {
   const SubDesc* subs;
   int nsubs;
   long long nitems;
+  const GroupDesc* groups;
+  int ngroups;
   const float* X;
   const uint8_t* fc;
   int n, d, G;
@@ -48,18 +50,20 @@ struct DensityLaunch {
   uint8_t* flags;
   unsigned* bitmaps;
   int words;
-  const long long* out_off;
-  int* out_ids;
-  float* out_acc;
+  const long long* loff;
+  int* lids;
+  float* lacc;
   unsigned long long* cand_counter;
 };
-void launch_density(const DensityLaunch& L, bool write, cudaStream_t s);
+void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s);
+void launch_density_flags(const DensityLaunch& L, cudaStream_t s);
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
                         cudaStream_t s);
 void launch_keep_compact(const SubDesc* subs, int nsubs, long long nitems, const uint8_t* flags, const int* cnt,
                          const long long* kpos, const long long* loff, const int* prev_keep, int* keep_ids,
                          long long* keep_loff, int* keep_lcnt, cudaStream_t s);
 void launch_word_popc(const unsigned* words, long long nw, int* out, cudaStream_t s);
+void launch_keep_popc(const unsigned* bm, int nsubs, int W, int* out, cudaStream_t s);
 void launch_gather_kstart(const SubDesc* subs, int nsubs, const long long* kpos, long long nitems, long long K,
                           long long* out, cudaStream_t s);
 void launch_gather_cbase(const long long* kstart, int nsubs, const int* root_id, long long K, int ncomp, int* out,
@@ -113,8 +117,9 @@ struct ClusterArgs {
 };
 void launch_uf_init(int* par, long long n, cudaStream_t s);
 void launch_uf_union(const ClusterArgs& a, cudaStream_t s);
-void launch_uf_flatten(const ClusterArgs& a, int* is_root, cudaStream_t s);
-void launch_comp_ids(const ClusterArgs& a, const int* root_id, int* comp, int* mcount, cudaStream_t s);
+void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s);
+void launch_comp_ids(const ClusterArgs& a, const int* root_id, const int* root_of, int* comp, int* mcount,
+                     cudaStream_t s);
 void launch_members(const ClusterArgs& a, const int* comp, const long long* moff, int* mfill, int* members,
                     cudaStream_t s);
 void launch_borders(const ClusterArgs& a, const int* comp, const int* cslot_of, int* slots, int2* ovf, int* novf,

@@ -107,36 +107,35 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a) {
   }
 }
 
-// flatten: every dense point points at its root; roots are flagged
-__global__ void k_uf_flatten(ClusterArgs a, int* is_root) {
+// roots: every dense point's root goes to a separate array (writing it into
+// `par` would race with the path-halving writes of concurrent finds, which
+// may store a non-root ancestor over it); roots are flagged
+__global__ void k_uf_flatten(ClusterArgs a, int* is_root, int* root_of) {
   long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
   int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
-  int root = 0;
+  int root = 0, r = -1;
   if (a.clustered[si]) {
     const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
     if (bit_of(dn, a.keep_ids[kk])) {
-      int r = uf_find(a.uf, (int)kk);
-      a.uf[kk] = r;
+      r = uf_find(a.uf, (int)kk);
       root = (r == (int)kk);
     }
   }
+  root_of[kk] = r;
   is_root[kk] = root;
 }
 
 // component id (global, dense) of every dense kept point; -1 otherwise
-__global__ void k_comp_ids(ClusterArgs a, const int* __restrict__ root_id, int* __restrict__ comp,
-                           int* __restrict__ mcount) {
+__global__ void k_comp_ids(ClusterArgs a, const int* __restrict__ root_id, const int* __restrict__ root_of,
+                           int* __restrict__ comp, int* __restrict__ mcount) {
   long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
-  int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  int r = root_of[kk];
   int c = -1;
-  if (a.clustered[si]) {
-    const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
-    if (bit_of(dn, a.keep_ids[kk])) {
-      c = root_id[a.uf[kk]];
-      atomicAdd(&mcount[c], 1);
-    }
+  if (r >= 0) {
+    c = root_id[r];
+    atomicAdd(&mcount[c], 1);
   }
   comp[kk] = c;
 }
@@ -277,11 +276,13 @@ void launch_uf_init(int* par, long long n, cudaStream_t s) {
 void launch_uf_union(const ClusterArgs& a, cudaStream_t s) {
   if (a.nkeep > 0) k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a);
 }
-void launch_uf_flatten(const ClusterArgs& a, int* is_root, cudaStream_t s) {
-  if (a.nkeep > 0) k_uf_flatten<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, is_root);
+void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s) {
+  if (a.nkeep > 0) k_uf_flatten<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, is_root, root_of);
 }
-void launch_comp_ids(const ClusterArgs& a, const int* root_id, int* comp, int* mcount, cudaStream_t s) {
-  if (a.nkeep > 0) k_comp_ids<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, root_id, comp, mcount);
+void launch_comp_ids(const ClusterArgs& a, const int* root_id, const int* root_of, int* comp, int* mcount,
+                     cudaStream_t s) {
+  if (a.nkeep > 0)
+    k_comp_ids<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, root_id, root_of, comp, mcount);
 }
 void launch_members(const ClusterArgs& a, const int* comp, const long long* moff, int* mfill, int* members,
                     cudaStream_t s) {

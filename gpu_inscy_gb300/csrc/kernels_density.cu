@@ -30,6 +30,9 @@ struct DensityArgs {
   const SubDesc* subs;
   int nsubs;
   long long nitems;
+  const GroupDesc* groups;  // children of one parent subspace, walked child-fastest
+  int ngroups;
+  long long nwarps;
   const float* X;
   const uint8_t* fc;
   int n, d, G;
@@ -48,15 +51,14 @@ struct DensityArgs {
   const int* prev_lids;
   const float* prev_lacc;
   // outputs
-  int* cnt;                 // [nitems]
-  uint8_t* flags;           // [nitems]
-  unsigned* bitmaps;        // per subspace 3 * W words (weak, dense, keep)
-  int words;                // W = ceil(n / 32)
-  // pass 2 (list output)
-  const long long* out_off;  // [nitems] list start of kept items
-  int* out_ids;
-  float* out_acc;
-  unsigned long long* cand_counter;  // candidates tested (pass 1)
+  int* cnt;           // [nitems] neighbours
+  uint8_t* flags;     // [nitems]
+  unsigned* bitmaps;  // per subspace 3 * W words (weak, dense, keep)
+  int words;          // W = ceil(n / 32)
+  const long long* loff;  // [nitems] list start of every item
+  int* lids;
+  float* lacc;
+  unsigned long long* cand_counter;  // candidates tested
 };
 
 __device__ __forceinline__ int find_sub(const SubDesc* subs, int nsubs, long long item) {
@@ -71,17 +73,36 @@ __device__ __forceinline__ int find_sub(const SubDesc* subs, int nsubs, long lon
   return lo;
 }
 
-template <bool kWrite>
-__global__ void __launch_bounds__(256) k_density(DensityArgs a) {
-  const long long item = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (item >= a.nitems) return;
-  const unsigned lane = lane_id();
-  const int si = find_sub(a.subs, a.nsubs, item);
-  const SubDesc S = a.subs[si];
-  const long long i = item - S.item_off;
-  const bool level1 = S.parent < 0;
-  if (kWrite && !(a.flags[item] & kFlagKeep)) return;
+// warp w -> (subspace, query index): the children of one parent are adjacent,
+// so the parent's list of a point is read by its siblings back to back (L2)
+__device__ __forceinline__ void locate(const DensityArgs& a, long long w, int& si, long long& i) {
+  int lo = 0, hi = a.ngroups - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.groups[mid].warp_off <= w)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const GroupDesc g = a.groups[lo];
+  long long j = w - g.warp_off;
+  i = j / g.nchild;
+  si = g.sub_base + (int)(j % g.nchild);
+}
 
+// count (kWrite = false) or write (kWrite = true) the ordered neighbour list
+// of one (subspace, point): candidates 32 at a time, accepted lanes by ballot
+template <bool kWrite>
+__global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= a.nwarps) return;
+  const unsigned lane = lane_id();
+  int si;
+  long long i;
+  locate(a, w, si, i);
+  const SubDesc& S = a.subs[si];
+  const long long item = S.item_off + i;
+  const bool level1 = S.parent < 0;
   const int D = S.dim;
   const int p = level1 ? (int)i : a.prev_keep[S.query_off + i];
   const float xp = a.X[(size_t)p * a.d + D];
@@ -99,10 +120,8 @@ __global__ void __launch_bounds__(256) k_density(DensityArgs a) {
     accs = a.prev_lacc + b;
     len = a.prev_lcnt[S.query_off + i];
   }
-
-  float sum = 0.f;
   int count = 0;
-  long long wbase = kWrite ? a.out_off[item] : 0;
+  const long long wbase = kWrite ? a.loff[item] : 0;
   for (long long j0 = 0; j0 < len; j0 += 32) {
     long long j = j0 + lane;
     bool ok = j < len;
@@ -112,48 +131,55 @@ __global__ void __launch_bounds__(256) k_density(DensityArgs a) {
       int fq = a.fc[(size_t)q * a.d + D];
       ok = fq >= fp - 1 && fq <= fp + 1;
     }
-    float acc2 = 0.f, dist = 0.f;
+    float acc2 = 0.f;
     if (ok) {
       float acc = level1 ? 0.f : accs[j];
       acc2 = dist_step(acc, xp, a.X[(size_t)q * a.d + D]);
-      dist = __fsqrt_rn(acc2);
-      ok = a.eps >= dist;
+      ok = a.eps >= __fsqrt_rn(acc2);
     }
     unsigned m = __ballot_sync(0xffffffffu, ok);
-    if (kWrite) {
-      if (ok) {
-        long long o = wbase + count + __popc(m & lanemask_lt());
-        a.out_ids[o] = q;
-        a.out_acc[o] = acc2;
-      }
-    } else if (!a.rect) {
-      double t = ok ? phi_term(dist, a.eps) : 0.0;
-      unsigned mm = m;
-      while (mm) {
-        int b = __ffs(mm) - 1;
-        mm &= mm - 1;
-        double tb = __shfl_sync(0xffffffffu, t, b);
-        sum = phi_add(sum, tb);
-      }
+    if (kWrite && ok) {
+      long long o = wbase + count + __popc(m & lanemask_lt());
+      a.lids[o] = q;
+      a.lacc[o] = acc2;
     }
     count += __popc(m);
   }
-  if (kWrite) return;
-  const float v = a.rect ? (float)count : sum;
+  if (!kWrite && lane == 0) {
+    a.cnt[item] = count;
+    if (a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len);
+  }
+}
+
+// density of one (subspace, point) from its list, one thread each (the phi
+// sum is sequential; every lane works on its own point)
+__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
+  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.nitems) return;
+  const int si = find_sub(a.subs, a.nsubs, item);
+  const SubDesc& S = a.subs[si];
+  const long long i = item - S.item_off;
+  const int p = S.parent < 0 ? (int)i : a.prev_keep[S.query_off + i];
+  const int c = a.cnt[item];
+  float v;
+  if (a.rect) {
+    v = (float)c;
+  } else {
+    const float* acc = a.lacc + a.loff[item];
+    float sum = 0.f;
+    for (int j = 0; j < c; ++j) sum = phi_add(sum, phi_term(__fsqrt_rn(acc[j]), a.eps));
+    v = sum;
+  }
   uint8_t f = 0;
   if (v >= a.thr_weak) f |= kFlagWeak;
   if (v >= a.thr_dense[S.nsub]) f |= kFlagDense;
   if (v >= a.thr_keep[S.nsub]) f |= kFlagKeep;
-  if (lane == 0) {
-    if (a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len);
-    a.cnt[item] = count;
-    a.flags[item] = f;
-    unsigned bit = 1u << (p & 31);
-    unsigned* bm = a.bitmaps + S.bitmap_off + (p >> 5);
-    if (f & kFlagWeak) atomicOr(bm, bit);
-    if (f & kFlagDense) atomicOr(bm + a.words, bit);
-    if (f & kFlagKeep) atomicOr(bm + 2 * a.words, bit);
-  }
+  a.flags[item] = f;
+  unsigned bit = 1u << (p & 31);
+  unsigned* bm = a.bitmaps + S.bitmap_off + (p >> 5);
+  if (f & kFlagWeak) atomicOr(bm, bit);
+  if (f & kFlagDense) atomicOr(bm + a.words, bit);
+  if (f & kFlagKeep) atomicOr(bm + 2 * a.words, bit);
 }
 
 // kept items: list lengths (0 for the others) for the offset scan
@@ -191,6 +217,19 @@ __global__ void k_word_popc(const unsigned* __restrict__ words, long long nw, in
   if (i < nw) out[i] = __popc(words[i]);
 }
 
+// popcount of the kept-bitmap words of every subspace (third bitmap of each)
+__global__ void k_keep_popc(const unsigned* __restrict__ bm, int nsubs, int W, int* __restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nsubs * W) return;
+  long long s = i / W, w = i % W;
+  out[i] = __popc(bm[s * 3 * W + 2 * W + w]);
+}
+
+void launch_keep_popc(const unsigned* bm, int nsubs, int W, int* out, cudaStream_t s) {
+  long long nw = (long long)nsubs * W;
+  if (nw > 0) k_keep_popc<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(bm, nsubs, W, out);
+}
+
 // first kept index of every subspace: the kept-prefix at its first item
 __global__ void k_gather_kstart(const SubDesc* __restrict__ subs, int nsubs, const long long* __restrict__ kpos,
                                 long long nitems, long long K, long long* __restrict__ out) {
@@ -223,12 +262,14 @@ void launch_gather_cbase(const long long* kstart, int nsubs, const int* root_id,
   k_gather_cbase<<<(nsubs + 1 + 255) / 256, 256, 0, s>>>(kstart, nsubs, root_id, K, ncomp, out);
 }
 
-void launch_density(const DensityLaunch& L, bool write, cudaStream_t s) {
-  if (L.nitems <= 0) return;
+static DensityArgs make_args(const DensityLaunch& L) {
   DensityArgs a;
   a.subs = L.subs;
   a.nsubs = L.nsubs;
   a.nitems = L.nitems;
+  a.groups = L.groups;
+  a.ngroups = L.ngroups;
+  a.nwarps = L.nitems;
   a.X = L.X;
   a.fc = L.fc;
   a.n = L.n;
@@ -250,16 +291,27 @@ void launch_density(const DensityLaunch& L, bool write, cudaStream_t s) {
   a.flags = L.flags;
   a.bitmaps = L.bitmaps;
   a.words = L.words;
-  a.out_off = L.out_off;
-  a.out_ids = L.out_ids;
-  a.out_acc = L.out_acc;
+  a.loff = L.loff;
+  a.lids = L.lids;
+  a.lacc = L.lacc;
   a.cand_counter = L.cand_counter;
-  long long threads = L.nitems * 32;
-  unsigned blocks = (unsigned)((threads + 255) / 256);
+  return a;
+}
+
+void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s) {
+  if (L.nitems <= 0) return;
+  DensityArgs a = make_args(L);
+  unsigned blocks = (unsigned)((L.nitems * 32 + 255) / 256);
   if (write)
-    k_density<true><<<blocks, 256, 0, s>>>(a);
+    k_neighbours<true><<<blocks, 256, 0, s>>>(a);
   else
-    k_density<false><<<blocks, 256, 0, s>>>(a);
+    k_neighbours<false><<<blocks, 256, 0, s>>>(a);
+}
+
+void launch_density_flags(const DensityLaunch& L, cudaStream_t s) {
+  if (L.nitems <= 0) return;
+  DensityArgs a = make_args(L);
+  k_density_flags<<<(unsigned)((L.nitems + 255) / 256), 256, 0, s>>>(a);
 }
 
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
