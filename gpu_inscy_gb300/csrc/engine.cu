@@ -661,7 +661,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       int nd = d - hcalls[i].f;
       for (int t = 0; t < nd; ++t) {
         work_scr.push_back(scr);
-        scr += 3LL * hcalls[i].npts + 1;
+        scr += 3LL * hcalls[i].npts + 1 + 2LL * hcalls[i].nghost;
       }
       nwork += nd;
       pts_cap += (long long)hcalls[i].npts * nd;
@@ -681,7 +681,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     int* dout_pts = next_pts->get<int>(pts_cap);
     unsigned long long* dtops = lv.get<unsigned long long>(2);
     int* derr = lv.get<int>(1);
-    long long ghost_cap = std::max(1024LL, ghost_in + pts_cap / 4);
+    long long ghost_cap = std::max(1024LL, ghost_in + 2 * pts_cap);
     int2* dout_gh = nullptr;
     std::vector<RegionRec> recs;
     std::vector<int> nrecs(nwork);

@@ -53,7 +53,7 @@ struct TreeArgs {
   int n, d, cells, min_size;
   const SubDesc* subs;
   const unsigned* bitmaps;
-  int* scratch;  // per work item: 3 * npts + 1 ints at work_scratch[w]
+  int* scratch;  // per work item: 3 * npts + 1 + 2 * nghost ints at work_scratch[w]
   const long long* work_scratch;
   RegionRec* recs;  // per work item: cells records
   int* nrecs;
@@ -175,6 +175,30 @@ __device__ __forceinline__ void prefix_range(const uint8_t* cc, int d, const int
   hi = a;
 }
 
+// [lo, hi) of the detached chains (indices into Gh, in leaf order of their
+// points) whose point shares i's first L remaining cells
+__device__ __forceinline__ void ghost_range(const uint8_t* cc, int d, const int* lam, const int2* Gh, const int* GI,
+                                            int m, int i, int L, int& lo, int& hi) {
+  int a = 0, b = m;
+  while (a < b) {
+    int mid = (a + b) >> 1;
+    if (cmp_prefix(cc, d, lam, Gh[GI[mid]].x, i, L) < 0)
+      a = mid + 1;
+    else
+      b = mid;
+  }
+  lo = a;
+  b = m;
+  while (a < b) {
+    int mid = (a + b) >> 1;
+    if (cmp_prefix(cc, d, lam, Gh[GI[mid]].x, i, L) <= 0)
+      a = mid + 1;
+    else
+      b = mid;
+  }
+  hi = a;
+}
+
 __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   __shared__ TreeShared s;
   const int w = blockIdx.x;
@@ -202,6 +226,8 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   int* A = a.scratch + a.work_scratch[w];
   int* B = A + np;
   int* SV = B + np;  // np + 1 survivor prefix counts
+  int* GA = SV + np + 1;  // ng: detached chains of the region, in leaf order
+  int* GB = GA + ng;
   RegionRec* rec = a.recs + (long long)w * a.cells;
 
   // 1. cell counts and s-connection flags on D
@@ -315,7 +341,44 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
           if (SV[j + 1] != SV[j]) a.out_pts[pts_off + SV[j]] = x;
         }
       }
-      // 6. ghosts of the pruned tree
+      // 6. ghosts of the pruned tree.  The region's detached chains (those
+      //    lying in the run, not starting on D), sorted into leaf order of
+      //    their points, answer "does a deeper chain pass this node" by
+      //    binary search.
+      int ngp = 0;
+      if (ng > 0 && !drop) {
+        for (int c = 0; c < ng; c += blockDim.x) {
+          int j = c + threadIdx.x;
+          int f = 0;
+          if (j < ng) {
+            int2 gg = Gh[j];
+            int cx = a.cc[(size_t)gg.x * d + D];
+            f = (gg.y != D && gg.y >= 0 && gg.y < d && ((lammask >> gg.y) & 1ull) && cx >= c0 && cx <= c1) ? 1 : 0;
+          }
+          int tot;
+          int inc = block_inclusive_scan<int>(f, s.sh, &tot);
+          if (f) GA[ngp + inc - 1] = j;
+          ngp += tot;
+        }
+        __syncthreads();
+        if (ngp > 1) {
+          int* gc = GA;
+          int* go = GB;
+          for (int l = nlam - 1; l >= 0; --l) {
+            const int k = s.lam[l];
+            block_sort_pass(
+                gc, go, ngp, [&](int j) { return (int)a.cc[(size_t)Gh[j].x * d + k]; }, a.cells, s.base, s.tot,
+                s.wc);
+            int* t = gc;
+            gc = go;
+            go = t;
+          }
+          if (gc != GA) {
+            for (int j = threadIdx.x; j < ngp; j += blockDim.x) GA[j] = gc[j];
+            __syncthreads();
+          }
+        }
+      }
       for (int phase = 0; phase < 2; ++phase) {
         if (threadIdx.x == 0) {
           if (phase == 0) s.gcount = 0;
@@ -345,12 +408,9 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
           }
         }
         // (b) ghosts detached earlier
-        for (int j = threadIdx.x; j < ng; j += blockDim.x) {
-          int2 gg = Gh[j];
+        for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
+          int2 gg = Gh[GA[jj]];
           int x = gg.x, g = gg.y;
-          if (g == D || g < 0 || g >= d || !((lammask >> g) & 1ull)) continue;
-          int cx = a.cc[(size_t)x * d + D];
-          if (cx < c0 || cx > c1 || drop) continue;
           int l = __popcll(lammask & ((1ull << g) - 1));
           int plo, phi;
           bool alive = true;
@@ -368,13 +428,11 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
           else {
             // the sibling node exists only if a deeper detached chain passes it
             keep = true;
-            for (int t = 0; t < ng; ++t) {
-              int2 h = Gh[t];
-              if (h.y == D || h.y < 0 || h.y >= d || !((lammask >> h.y) & 1ull)) continue;
-              int ch = a.cc[(size_t)h.x * d + D];
-              if (ch < c0 || ch > c1) continue;
-              int lh = __popcll(lammask & ((1ull << h.y) - 1));
-              if (lh > l && cmp_prefix(a.cc, d, s.lam, h.x, x, l + 1) == 0) {
+            int glo, ghi;
+            ghost_range(a.cc, d, s.lam, Gh, GA, ngp, x, l + 1, glo, ghi);
+            for (int t = glo; t < ghi; ++t) {
+              int lh = __popcll(lammask & ((1ull << Gh[GA[t]].y) - 1));
+              if (lh > l) {
                 keep = false;
                 break;
               }
