@@ -240,7 +240,8 @@ def main():
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats_all)),
             "roofline": roof, "clocks": clk,
             "breakdown_ms": {k: st[k] for k in ("ms_setup", "ms_density", "ms_density_pass1", "ms_tree",
-                                               "ms_cluster", "ms_replay", "ms_total")},
+                                               "ms_cluster", "ms_replay", "ms_replay_prune", "ms_replay_cluster",
+                                               "ms_replay_join", "ms_d2h", "ms_total")},
             "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
             "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}
     if rank == 0 and not args.no_cpu_baseline:

@@ -35,7 +35,7 @@ class Params(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_double) for name in
                 ("ms_total", "ms_setup", "ms_density", "ms_density_pass1", "ms_tree", "ms_cluster", "ms_replay",
-                 "density_bytes", "tree_bytes")] + \
+                 "ms_replay_prune", "ms_replay_cluster", "ms_replay_join", "ms_d2h", "density_bytes", "tree_bytes")] + \
                [(name, ctypes.c_longlong) for name in
                 ("density_launches_pass1", "kernel_launches", "calls", "regions", "subspaces", "candidates",
                  "levels", "h2d_bytes", "d2h_bytes")]

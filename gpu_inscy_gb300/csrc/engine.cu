@@ -195,7 +195,8 @@ struct HCall {
   int level = 0;
   int npts = 0;
   long long pts_off = 0;  // into levels_[level].pts (its leaf order)
-  int norder = 0;         // components in first-seed order, at levels_[level].order[pts_off ...]
+  int norder = 0;         // components in first-seed order, at levels_[level].order[order_off ...]
+  long long order_off = 0;
   int csub = -1;          // clustered subspace (its own subspace) in subs_
   std::vector<HRegion> regions;  // ordered by (dim, cell run)
 };
@@ -262,11 +263,13 @@ class Engine {
   }
   void d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     if (!bytes) return;
+    auto t0 = std::chrono::steady_clock::now();
     void* st = pinned_.get(bytes);
     CK(cudaMemcpyAsync(st, src, bytes, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     std::memcpy(dst, st, bytes);
     stats_.d2h_bytes += (long long)bytes;
+    stats_.ms_d2h += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   void h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     if (!bytes) return;
@@ -310,6 +313,7 @@ class Engine {
   std::map<uint64_t, int> eidx_;              // subspace -> entry
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<std::vector<int>> vbuf_;        // one n-vector of labels per recursion depth
+  double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
   inscy_stats stats_;
 };
 
@@ -782,7 +786,6 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     if (!ncall.empty()) {
       hl.pts.resize(tops[0]);
       d2h(hl.pts.data(), dout_pts, sizeof(int) * tops[0], s);
-      hl.order.assign(tops[0], 0);
       std::vector<uint8_t> clustered(nsubs, 0);
       std::vector<std::vector<int>> sub_calls(nsubs);
       for (size_t j = 0; j < ncall.size(); ++j) {
@@ -907,9 +910,20 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       std::vector<int> hmem(hm[0]), hbor(hb);
       d2h(hmem.data(), members, sizeof(int) * hm[0], s);
       d2h(hbor.data(), borders, sizeof(int) * hb, s);
-      d2h(hl.order.data(), order, sizeof(int) * tops[0], s);
       std::vector<int> hocnt(ncall.size());
+      long long* order_off = lv.get<long long>(ncall.size() + 1);
+      long long* dot = lv.get<long long>(1);
+      launch_exclusive_scan_i2ll(order_cnt, order_off, (long long)ncall.size(), dot,
+                                 scan_sums((long long)ncall.size() + 1, s, lv), s);
+      const long long norder_tot = scalar(dot, s);
+      int* packed = lv.get<int>(norder_tot + 1);
+      launch_pack_order(dncall, (int)ncall.size(), order, order_cnt, order_off, packed, s);
+      launches += 4;
+      hl.order.resize(norder_tot);
+      d2h(hl.order.data(), packed, sizeof(int) * norder_tot, s);
       d2h(hocnt.data(), order_cnt, sizeof(int) * ncall.size(), s);
+      std::vector<long long> hooff(ncall.size());
+      d2h(hooff.data(), order_off, sizeof(long long) * ncall.size(), s);
       // one HSub per clustered subspace (component-local offsets)
       std::vector<int> csub_of(nsubs, -1);
       for (int i : clist) {
@@ -930,6 +944,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         HCall& hc = calls_[ncall_ids[j]];
         hc.csub = csub_of[ncall[j].sub];
         hc.norder = hocnt[j];
+        hc.order_off = hooff[j];
       }
     }
 
@@ -959,7 +974,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   auto t_rep0 = std::chrono::steady_clock::now();
   vbuf_.assign(d + 2, std::vector<int>());
   tbits_.assign(((size_t)n + 63) / 64, 0);
+  t_prune_ = t_cluster_ = t_join_ = 0;
   replay(0);
+  stats_.ms_replay_prune = t_prune_;
+  stats_.ms_replay_cluster = t_cluster_;
+  stats_.ms_replay_join = t_join_;
   stats_.ms_replay = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_rep0).count();
   {
     // the result map's order (vec_cmp)
@@ -999,9 +1018,17 @@ void Engine::replay(int ci) {
       const HRegion R = calls_[ci].regions[ri++];
       if (!R.passed) continue;
       replay(R.child);
-      if (prune_redundancy(calls_[R.child], smask)) cluster_into(calls_[R.child], V, touched, nlabels);
+      auto t0 = std::chrono::steady_clock::now();
+      bool ok = prune_redundancy(calls_[R.child], smask);
+      auto t1 = std::chrono::steady_clock::now();
+      if (ok) cluster_into(calls_[R.child], V, touched, nlabels);
+      auto t2 = std::chrono::steady_clock::now();
+      t_prune_ += std::chrono::duration<double, std::milli>(t1 - t0).count();
+      t_cluster_ += std::chrono::duration<double, std::milli>(t2 - t1).count();
     }
+    auto t3 = std::chrono::steady_clock::now();
     join(V, touched, nlabels, smask);
+    t_join_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t3).count();
     for (int p : touched) V[p] = -1;
   }
 }
@@ -1074,7 +1101,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
 // next label, non-dense neighbours that are still -1 become -2.
 void Engine::cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>& touched, int& nlabels) {
   const HSub& hs = subs_[c.csub];
-  const int* order = levels_[c.level].order.data() + c.pts_off;
+  const int* order = levels_[c.level].order.data() + c.order_off;
   for (int t = 0; t < c.norder; ++t) {
     int comp = order[t];
     long long m0 = hs.moff[comp], m1 = hs.moff[comp + 1];

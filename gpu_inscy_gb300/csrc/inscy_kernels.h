@@ -131,4 +131,7 @@ void launch_region_order(const ClusterArgs& a, int nclustered, const int* comp, 
                          const int* sub_calls_off, const int* sub_calls, const CallDesc* ncalls, const int* pts,
                          int* firstpos, int* order, int* order_cnt, cudaStream_t s);
 
+void launch_pack_order(const CallDesc* ncalls, int ncall, const int* order, const int* order_cnt,
+                       const long long* order_off, int* packed, cudaStream_t s);
+
 }  // namespace inscy

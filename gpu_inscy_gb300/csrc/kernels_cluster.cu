@@ -269,6 +269,22 @@ __global__ void __launch_bounds__(256) k_region_order(ClusterArgs a, const int* 
   }
 }
 
+// pack the per-region component orders (written at each region's point
+// offset) into consecutive lists
+__global__ void k_pack_order(const CallDesc* __restrict__ ncalls, int ncall, const int* __restrict__ order,
+                             const int* __restrict__ order_cnt, const long long* __restrict__ order_off,
+                             int* __restrict__ packed) {
+  const int c = blockIdx.x;
+  if (c >= ncall) return;
+  const long long src = ncalls[c].pts_off, dst = order_off[c];
+  for (int j = threadIdx.x; j < order_cnt[c]; j += blockDim.x) packed[dst + j] = order[src + j];
+}
+
+void launch_pack_order(const CallDesc* ncalls, int ncall, const int* order, const int* order_cnt,
+                       const long long* order_off, int* packed, cudaStream_t s) {
+  if (ncall > 0) k_pack_order<<<ncall, 128, 0, s>>>(ncalls, ncall, order, order_cnt, order_off, packed);
+}
+
 // ---------------------------------------------------------------------------
 void launch_uf_init(int* par, long long n, cudaStream_t s) {
   if (n > 0) k_uf_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(par, n);

@@ -64,7 +64,11 @@ typedef struct inscy_stats {
   double ms_tree;           /* restrict/merge/prune kernels, device time */
   double ms_cluster;        /* union-find + component kernels, device time */
   double ms_replay;         /* host commit (pruneRedundancy, numbering, join) */
-  double density_bytes;     /* algorithmic bytes of the density pass-1 launches */
+  double ms_replay_prune;   /* ... of which pruneRedundancy */
+  double ms_replay_cluster; /* ... of which cluster numbering */
+  double ms_replay_join;    /* ... of which join */
+  double ms_d2h;            /* device-to-host copies (synchronous, host clock) */
+  double density_bytes;     /* algorithmic bytes of the density count launches */
   double tree_bytes;        /* algorithmic bytes of the tree launches */
   long long density_launches_pass1;
   long long kernel_launches; /* kernels launched by this run */
