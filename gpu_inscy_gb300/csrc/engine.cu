@@ -293,6 +293,7 @@ class Engine {
   // commit
   void replay(int ci);
   bool prune_redundancy(const HCall& c, uint64_t smask);
+  const std::vector<int>& superset_candidates(uint64_t smask);
   void cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>& touched, int& nlabels);
   void join(std::vector<int>& V, std::vector<int>& touched, int nlabels, uint64_t smask);
 
@@ -311,6 +312,7 @@ class Engine {
   std::vector<std::unique_ptr<Entry>> ents_;  // result map entries, in insertion order
   std::vector<uint64_t> emask_;               // their subspaces
   std::map<uint64_t, int> eidx_;              // subspace -> entry
+  std::vector<std::vector<int>> by_dim_;      // entries whose subspace holds each dim
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<std::vector<int>> vbuf_;        // one n-vector of labels per recursion depth
   double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
@@ -331,6 +333,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   ents_.clear();
   emask_.clear();
   eidx_.clear();
+  by_dim_.assign(d, std::vector<int>());
   out_dims.clear();
   out_labels.clear();
   if (n == 0) {
@@ -1040,6 +1043,29 @@ void Engine::replay(int ci) {
 // is decided; per entry the smallest touched cluster is found either by
 // scanning the region's points or, for large regions, by walking the entry's
 // clusters smallest-first against a bitmap of the region.
+// entries that may contain subspace `smask`: those holding its rarest dim
+const std::vector<int>& Engine::superset_candidates(uint64_t smask) {
+  int best = -1;
+  size_t bs = SIZE_MAX;
+  for (uint64_t m = smask; m; m &= m - 1) {
+    int k = __builtin_ctzll(m);
+    if (by_dim_[k].size() < bs) {
+      bs = by_dim_[k].size();
+      best = k;
+    }
+  }
+  return by_dim_[best];
+}
+
+static void refresh_order(Entry& E) {
+  if (!E.dirty) return;
+  E.by_size.clear();
+  for (int l = 0; l < (int)E.size.size(); ++l)
+    if (E.size[l] > 0) E.by_size.push_back(l);
+  std::stable_sort(E.by_size.begin(), E.by_size.end(), [&](int a, int b) { return E.size[a] < E.size[b]; });
+  E.dirty = false;
+}
+
 bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
   const int* pts = levels_[c.level].pts.data() + c.pts_off;
   const int m = c.npts;
@@ -1049,8 +1075,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
     for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] |= 1ull << (pts[j] & 63);
   int max_min = 0;
   bool result = true;
-  const size_t ne = ents_.size();
-  for (size_t i = 0; i < ne; ++i) {
+  for (int i : superset_candidates(smask)) {
     if ((emask_[i] & smask) != smask) continue;
     Entry& E = *ents_[i];
     int mn = -1;
@@ -1063,13 +1088,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
         }
       }
     } else {
-      if (E.dirty) {
-        E.by_size.clear();
-        for (int l = 0; l < (int)E.size.size(); ++l)
-          if (E.size[l] > 0) E.by_size.push_back(l);
-        std::stable_sort(E.by_size.begin(), E.by_size.end(), [&](int a, int b) { return E.size[a] < E.size[b]; });
-        E.dirty = false;
-      }
+      refresh_order(E);
       for (int l : E.by_size) {
         bool hit = false;
         for (int q : E.mem[l])
@@ -1142,21 +1161,37 @@ void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, u
     }
   if (minsz == INT32_MAX) return;
   std::vector<char> drop(nlabels + 1, 0);
-  const size_t ne = ents_.size();
-  for (size_t i = 0; i < ne; ++i) {
+  for (int i : superset_candidates(smask)) {
     if ((emask_[i] & smask) != smask) continue;
-    const Entry& H = *ents_[i];
-    // nothing can be dropped when even the smallest cluster times r is not
-    // below the entry's largest cluster (float comparisons as the reference)
-    if (hp_.r >= 0.f && !((float)minsz * hp_.r < (float)H.maxsz)) continue;
+    Entry& H = *ents_[i];
     bool hit = false;
-    for (int p : touched) {
-      int c = V[p];
-      if (c < 0) continue;
-      int h = H.lab[p];
-      if (h >= 0 && (float)sizes[c] * hp_.r < (float)H.size[h]) {
-        drop[c] = 1;
-        hit = true;
+    if (hp_.r >= 0.f) {
+      // only clusters of H larger than (smallest cluster here) * r can drop
+      // anything; walk them largest first (float comparisons as the reference)
+      if (!((float)minsz * hp_.r < (float)H.maxsz)) continue;
+      refresh_order(H);
+      for (int t = (int)H.by_size.size() - 1; t >= 0; --t) {
+        const int l = H.by_size[t];
+        const int hs = H.size[l];
+        if (!((float)minsz * hp_.r < (float)hs)) break;
+        for (int q : H.mem[l]) {
+          if (H.lab[q] != l) continue;
+          int c = V[q];
+          if (c >= 0 && (float)sizes[c] * hp_.r < (float)hs) {
+            drop[c] = 1;
+            hit = true;
+          }
+        }
+      }
+    } else {
+      for (int p : touched) {
+        int c = V[p];
+        if (c < 0) continue;
+        int h = H.lab[p];
+        if (h >= 0 && (float)sizes[c] * hp_.r < (float)H.size[h]) {
+          drop[c] = 1;
+          hit = true;
+        }
       }
     }
     if (hit) {
@@ -1180,6 +1215,7 @@ void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, u
     ne->lab.assign(n_, -1);
     E = ne.get();
     eidx_[smask] = (int)ents_.size();
+    for (uint64_t m = smask; m; m &= m - 1) by_dim_[__builtin_ctzll(m)].push_back((int)ents_.size());
     ents_.push_back(std::move(ne));
     emask_.push_back(smask);
     off = 0;
