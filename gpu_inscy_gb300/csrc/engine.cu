@@ -346,6 +346,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   if (G > 256) throw Error(INSCY_ERR_LIMIT, "ceil(1/neighborhood_size) = " + std::to_string(G) + " > 256");
   const float csz = 1.0f / (float)cells;
   const float fsz = 1.0f / (float)G;
+  // leaf keys pack one cell per dim into 128 bits
+  int kbits = 1;
+  while ((1 << kbits) < cells) ++kbits;
+  if (d * kbits > 128)
+    throw Error(INSCY_ERR_LIMIT, "d * ceil(log2(number_of_cells)) = " + std::to_string(d * kbits) + " > 128");
   const int W = (ni + 31) / 32;
   long long launches = 0;
 
@@ -668,7 +673,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       int nd = d - hcalls[i].f;
       for (int t = 0; t < nd; ++t) {
         work_scr.push_back(scr);
-        scr += 3LL * hcalls[i].npts + 1 + 2LL * hcalls[i].nghost;
+        // keys (16 B) of points and chains, then ints (see k_tree_level)
+        long long bytes = 16LL * (2LL * hcalls[i].npts + 2LL * hcalls[i].nghost) +
+                          4LL * (3LL * hcalls[i].npts + 1 + 2LL * hcalls[i].nghost);
+        scr += (bytes + 15) / 16 * 16;
       }
       nwork += nd;
       pts_cap += (long long)hcalls[i].npts * nd;
@@ -681,7 +689,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     h2d(dwork, work_off.data(), sizeof(long long) * ncalls, s);
     long long* dwscr = lv.get<long long>(nwork);
     h2d(dwscr, work_scr.data(), sizeof(long long) * nwork, s);
-    int* dscr = lv.get<int>(scr);
+    char* dscr = lv.get<char>(scr);
     RegionRec* drecs = lv.get<RegionRec>((size_t)nwork * cells);
     int* dnrecs = lv.get<int>(nwork);
     std::unique_ptr<Scope> next_pts(new Scope(*pool_, s));
@@ -710,6 +718,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       TL.d = d;
       TL.cells = cells;
       TL.min_size = hp.min_size;
+      TL.kbits = kbits;
       TL.subs = dsubs;
       TL.bitmaps = dbm;
       TL.scratch = dscr;

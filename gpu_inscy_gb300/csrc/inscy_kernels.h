@@ -80,9 +80,10 @@ struct TreeLaunch {
   const uint8_t* cc;
   const unsigned long long* gz;
   int n, d, cells, min_size;
+  int kbits;
   const SubDesc* subs;
   const unsigned* bitmaps;
-  int* scratch;
+  char* scratch;
   const long long* work_scratch;
   RegionRec* recs;
   int* nrecs;

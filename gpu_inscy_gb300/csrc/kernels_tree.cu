@@ -41,6 +41,8 @@ namespace inscy {
 constexpr int kTreeThreads = 256;
 constexpr int kTreeWarps = kTreeThreads / 32;
 
+using Key = unsigned __int128;
+
 struct TreeArgs {
   const CallDesc* calls;
   int ncalls;
@@ -51,9 +53,10 @@ struct TreeArgs {
   const uint8_t* cc;
   const unsigned long long* gz;
   int n, d, cells, min_size;
+  int kbits;  // bits per cell in the packed leaf keys
   const SubDesc* subs;
   const unsigned* bitmaps;
-  int* scratch;  // per work item: 3 * npts + 1 + 2 * nghost ints at work_scratch[w]
+  char* scratch;  // per work item, at work_scratch[w] bytes: see k_tree_level
   const long long* work_scratch;
   RegionRec* recs;  // per work item: cells records
   int* nrecs;
@@ -81,20 +84,32 @@ __device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) 
   return base;
 }
 
-// one stable counting-sort pass by digit(x) in [0, R)
-template <class Dig>
-__device__ void block_sort_pass(const int* in, int* out, int n, Dig dig, int R, int* s_base, int* s_tot, int* s_wc) {
+// one stable counting-sort pass of (key, value) pairs by an 8-bit digit of
+// the key (warp match for the intra-warp rank, block scan across warps)
+__device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* vout, int n, int shift, int* s_base,
+                                int* s_tot, int* s_wc) {
+  const int R = 256;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < R; i += blockDim.x) s_base[i] = 0;
   __syncthreads();
-  for (int j = threadIdx.x; j < n; j += blockDim.x) atomicAdd(&s_base[dig(in[j])], 1);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) atomicAdd(&s_base[(int)(kin[j] >> shift) & 255], 1);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int i = 0; i < R; ++i) {
-      int t = s_base[i];
-      s_base[i] = run;
-      run += t;
+  if (threadIdx.x < 32) {
+    // exclusive scan of the 256 digit counts by one warp
+    int v[8], run = 0;
+    for (int t = 0; t < 8; ++t) {
+      v[t] = s_base[lane * 8 + t];
+      run += v[t];
+    }
+    int inc = run;
+    for (int o = 1; o < 32; o <<= 1) {
+      int u = __shfl_up_sync(0xffffffffu, inc, o);
+      if ((int)lane >= o) inc += u;
+    }
+    int ex = inc - run;
+    for (int t = 0; t < 8; ++t) {
+      s_base[lane * 8 + t] = ex;
+      ex += v[t];
     }
   }
   __syncthreads();
@@ -103,8 +118,9 @@ __device__ void block_sort_pass(const int* in, int* out, int n, Dig dig, int R, 
     __syncthreads();
     int j = c0 + threadIdx.x;
     bool valid = j < n;
-    int x = valid ? in[j] : 0;
-    int v = valid ? dig(x) : R + (int)lane;
+    Key k = valid ? kin[j] : (Key)0;
+    int x = valid ? vin[j] : 0;
+    int v = valid ? ((int)(k >> shift) & 255) : R + (int)lane;
     unsigned peers = __match_any_sync(0xffffffffu, v);
     int rank = __popc(peers & lanemask_lt());
     if (valid && rank == 0) s_wc[warp * R + v] = __popc(peers);
@@ -119,7 +135,11 @@ __device__ void block_sort_pass(const int* in, int* out, int n, Dig dig, int R, 
       s_tot[u] = run;
     }
     __syncthreads();
-    if (valid) out[s_base[v] + s_wc[warp * R + v] + rank] = x;
+    if (valid) {
+      int o = s_base[v] + s_wc[warp * R + v] + rank;
+      kout[o] = k;
+      vout[o] = x;
+    }
     __syncthreads();
     for (int u = threadIdx.x; u < R; u += blockDim.x) s_base[u] += s_tot[u];
     __syncthreads();
@@ -143,22 +163,22 @@ struct TreeShared {
   int gwrite;
 };
 
-// compare the cells of points a and b on the first L remaining dims
-__device__ __forceinline__ int cmp_prefix(const uint8_t* cc, int d, const int* lam, int a, int b, int L) {
-  for (int t = 0; t < L; ++t) {
-    int x = cc[(size_t)a * d + lam[t]], y = cc[(size_t)b * d + lam[t]];
-    if (x != y) return x < y ? -1 : 1;
-  }
-  return 0;
+// leaf key of point x: its cells on the remaining dims (in level order, most
+// significant first), then its cell on the restricted dim D
+__device__ __forceinline__ Key leaf_key(const uint8_t* cc, int d, const int* lam, int nlam, int D, int b, int x) {
+  const uint8_t* row = cc + (size_t)x * d;
+  Key k = 0;
+  for (int t = 0; t < nlam; ++t) k = (k << b) | (Key)row[lam[t]];
+  return (k << b) | (Key)row[D];
 }
 
-// [lo, hi) of the points of A (leaf order) sharing i's first L remaining cells
-__device__ __forceinline__ void prefix_range(const uint8_t* cc, int d, const int* lam, const int* A, int m, int i,
-                                             int L, int& lo, int& hi) {
+// [lo, hi) of the keys of K[0..m) that share `key`'s prefix above bit `sh`
+__device__ __forceinline__ void key_range(const Key* K, int m, Key key, int sh, int& lo, int& hi) {
+  const Key pre = key >> sh;
   int a = 0, b = m;
   while (a < b) {
     int mid = (a + b) >> 1;
-    if (cmp_prefix(cc, d, lam, A[mid], i, L) < 0)
+    if ((K[mid] >> sh) < pre)
       a = mid + 1;
     else
       b = mid;
@@ -167,31 +187,7 @@ __device__ __forceinline__ void prefix_range(const uint8_t* cc, int d, const int
   b = m;
   while (a < b) {
     int mid = (a + b) >> 1;
-    if (cmp_prefix(cc, d, lam, A[mid], i, L) <= 0)
-      a = mid + 1;
-    else
-      b = mid;
-  }
-  hi = a;
-}
-
-// [lo, hi) of the detached chains (indices into Gh, in leaf order of their
-// points) whose point shares i's first L remaining cells
-__device__ __forceinline__ void ghost_range(const uint8_t* cc, int d, const int* lam, const int2* Gh, const int* GI,
-                                            int m, int i, int L, int& lo, int& hi) {
-  int a = 0, b = m;
-  while (a < b) {
-    int mid = (a + b) >> 1;
-    if (cmp_prefix(cc, d, lam, Gh[GI[mid]].x, i, L) < 0)
-      a = mid + 1;
-    else
-      b = mid;
-  }
-  lo = a;
-  b = m;
-  while (a < b) {
-    int mid = (a + b) >> 1;
-    if (cmp_prefix(cc, d, lam, Gh[GI[mid]].x, i, L) <= 0)
+    if ((K[mid] >> sh) <= pre)
       a = mid + 1;
     else
       b = mid;
@@ -216,6 +212,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   const CallDesc C = a.calls[ci];
   const int D = C.f + (int)(w - a.work_off[ci]);
   const int d = a.d;
+  const int b = a.kbits;
   const int* P = a.pts_in + C.pts_off;
   const int np = C.npts;
   const int2* Gh = a.ghosts_in + C.ghost_off;
@@ -223,10 +220,16 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   const uint64_t smask = C.rmask | (1ull << D);
   const SubDesc& S = a.subs[C.child_sub + (D - C.f)];
   const unsigned* wd = a.bitmaps + S.bitmap_off;
-  int* A = a.scratch + a.work_scratch[w];
+  // scratch: keys first (16-byte aligned), then ints
+  char* base = a.scratch + a.work_scratch[w];
+  Key* KA = (Key*)base;  // np: leaf keys of the region's points
+  Key* KB = KA + np;     // np
+  Key* KG = KB + np;     // ng: leaf keys of the region's detached chains
+  Key* KH = KG + ng;     // ng
+  int* A = (int*)(KH + ng);  // np: the region's points
   int* B = A + np;
-  int* SV = B + np;  // np + 1 survivor prefix counts
-  int* GA = SV + np + 1;  // ng: detached chains of the region, in leaf order
+  int* SV = B + np;       // np + 1 survivor prefix counts
+  int* GA = SV + np + 1;  // ng: detached chains of the region
   int* GB = GA + ng;
   RegionRec* rec = a.recs + (long long)w * a.cells;
 
@@ -269,6 +272,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   const int nruns = s.nruns;
   const int nlam = s.nlam;
   const bool last_dim = (C.nrestricted + 1 == d);
+  const int key_bits = (nlam + 1) * b;
   uint64_t lammask = ~smask;
   if (d < 64) lammask &= (1ull << d) - 1;
 
@@ -285,21 +289,21 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
             return c >= c0 && c <= c1;
           },
           A, s.sh);
+    for (int j = threadIdx.x; j < m; j += blockDim.x) KA[j] = leaf_key(a.cc, d, s.lam, nlam, D, b, A[j]);
     __syncthreads();
-    // 4. merged runs: stable re-sort into (remaining cells, cell on D) order
+    // 4. merged runs: stable re-sort by the leaf key (remaining cells, cell on
+    //    D); equal keys keep their order (the restricted dims, then id)
+    Key* kcur = KA;
     int* cur = A;
     if (c1 > c0 && m > 1) {
+      Key* koth = KB;
       int* oth = B;
-      block_sort_pass(
-          cur, oth, m, [&](int x) { return (int)a.cc[(size_t)x * d + D]; }, a.cells, s.base, s.tot, s.wc);
-      int* t = cur;
-      cur = oth;
-      oth = t;
-      for (int l = nlam - 1; l >= 0; --l) {
-        const int k = s.lam[l];
-        block_sort_pass(
-            cur, oth, m, [&](int x) { return (int)a.cc[(size_t)x * d + k]; }, a.cells, s.base, s.tot, s.wc);
-        t = cur;
+      for (int sh = 0; sh < key_bits; sh += 8) {
+        block_sort_pass(kcur, cur, koth, oth, m, sh, s.base, s.tot, s.wc);
+        Key* tk = kcur;
+        kcur = koth;
+        koth = tk;
+        int* t = cur;
         cur = oth;
         oth = t;
       }
@@ -342,9 +346,9 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
         }
       }
       // 6. ghosts of the pruned tree.  The region's detached chains (those
-      //    lying in the run, not starting on D), sorted into leaf order of
-      //    their points, answer "does a deeper chain pass this node" by
-      //    binary search.
+      //    lying in the run, not starting on D) are sorted by the leaf key of
+      //    their points, so "does a deeper chain pass this node" is a range
+      //    search too.
       int ngp = 0;
       if (ng > 0 && !drop) {
         for (int c = 0; c < ng; c += blockDim.x) {
@@ -361,20 +365,27 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
           ngp += tot;
         }
         __syncthreads();
+        for (int j = threadIdx.x; j < ngp; j += blockDim.x) KG[j] = leaf_key(a.cc, d, s.lam, nlam, D, b, Gh[GA[j]].x);
+        __syncthreads();
         if (ngp > 1) {
+          Key* kc = KG;
+          Key* ko = KH;
           int* gc = GA;
           int* go = GB;
-          for (int l = nlam - 1; l >= 0; --l) {
-            const int k = s.lam[l];
-            block_sort_pass(
-                gc, go, ngp, [&](int j) { return (int)a.cc[(size_t)Gh[j].x * d + k]; }, a.cells, s.base, s.tot,
-                s.wc);
+          for (int sh = 0; sh < key_bits; sh += 8) {
+            block_sort_pass(kc, gc, ko, go, ngp, sh, s.base, s.tot, s.wc);
+            Key* tk = kc;
+            kc = ko;
+            ko = tk;
             int* t = gc;
             gc = go;
             go = t;
           }
           if (gc != GA) {
-            for (int j = threadIdx.x; j < ngp; j += blockDim.x) GA[j] = gc[j];
+            for (int j = threadIdx.x; j < ngp; j += blockDim.x) {
+              GA[j] = gc[j];
+              KG[j] = kc[j];
+            }
             __syncthreads();
           }
         }
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
             gb &= gb - 1;
             int l = __popcll(lammask & ((1ull << g) - 1));
             int plo, phi;
-            prefix_range(a.cc, d, s.lam, cur, m, x, l + 1, plo, phi);
+            key_range(kcur, m, kcur[j], b * (nlam - l), plo, phi);  // prefix through level l
             if (SV[phi] - SV[plo] > 0) {
               if (phase == 0)
                 atomicAdd(&s.gcount, 1);
@@ -411,15 +422,16 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
         for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
           int2 gg = Gh[GA[jj]];
           int x = gg.x, g = gg.y;
+          const Key kx = KG[jj];
           int l = __popcll(lammask & ((1ull << g) - 1));
           int plo, phi;
           bool alive = true;
           if (l > 0) {
-            prefix_range(a.cc, d, s.lam, cur, m, x, l, plo, phi);
+            key_range(kcur, m, kx, b * (nlam - l + 1), plo, phi);  // prefix through level l-1
             alive = SV[phi] - SV[plo] > 0;
           }
           if (!alive) continue;
-          prefix_range(a.cc, d, s.lam, cur, m, x, l + 1, plo, phi);
+          key_range(kcur, m, kx, b * (nlam - l), plo, phi);
           bool keep;
           if (SV[phi] - SV[plo] > 0)
             keep = true;  // the sibling node keeps points
@@ -429,7 +441,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
             // the sibling node exists only if a deeper detached chain passes it
             keep = true;
             int glo, ghi;
-            ghost_range(a.cc, d, s.lam, Gh, GA, ngp, x, l + 1, glo, ghi);
+            key_range(KG, ngp, kx, b * (nlam - l), glo, ghi);
             for (int t = glo; t < ghi; ++t) {
               int lh = __popcll(lammask & ((1ull << Gh[GA[t]].y) - 1));
               if (lh > l) {
@@ -499,6 +511,7 @@ void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
   a.d = L.d;
   a.cells = L.cells;
   a.min_size = L.min_size;
+  a.kbits = L.kbits;
   a.subs = L.subs;
   a.bitmaps = L.bitmaps;
   a.scratch = L.scratch;
