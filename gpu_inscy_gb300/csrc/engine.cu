@@ -213,16 +213,31 @@ struct HSub {  // components of one clustered subspace
   std::vector<int> borders;
 };
 
+// Where the points of a label come from: component `comp` of clustered
+// subspace `csub` (its member list is the GPU's).
+struct LabelRef {
+  int csub;
+  int comp;
+};
+
 // One result-map entry (a clustered subspace) during the commit.
 struct Entry {
   uint64_t mask = 0;
-  std::vector<int> lab;             // one label per point (-1 noise, -2 border)
-  std::vector<int> size;            // points per label (index = label)
-  std::vector<std::vector<int>> mem;  // points ever given each label (validated lazily)
-  int maxv = -100000;               // v_max(lab) (util.cu:566-574)
-  int maxsz = 0;                    // largest cluster
-  std::vector<int> by_size;         // labels in ascending size (rebuilt when dirty)
+  std::vector<int> lab;        // one label per point (-1 noise, -2 border)
+  std::vector<int> size;       // points per label (index = label)
+  std::vector<LabelRef> src;   // members of each label (may include points relabelled since)
+  int maxv = -100000;          // v_max(lab) (util.cu:566-574)
+  int maxsz = 0;               // largest cluster
+  std::vector<int> by_size;    // labels in ascending size (rebuilt when dirty)
   bool dirty = true;
+};
+
+// The clusters numbered in one dim loop (the reference's shared clustering
+// vector): label l -> component, and its size.
+struct LoopState {
+  std::vector<LabelRef> ref{LabelRef{-1, -1}};
+  std::vector<int> size{0};
+  int nlabels = 0;
 };
 
 struct HostParams {
@@ -294,8 +309,8 @@ class Engine {
   void replay(int ci);
   bool prune_redundancy(const HCall& c, uint64_t smask);
   const std::vector<int>& superset_candidates(uint64_t smask);
-  void cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>& touched, int& nlabels);
-  void join(std::vector<int>& V, std::vector<int>& touched, int nlabels, uint64_t smask);
+  void cluster_into(const HCall& c, std::vector<int>& V, LoopState& st);
+  void join(std::vector<int>& V, LoopState& st, uint64_t smask);
 
   int device_ = 0;
   std::unique_ptr<Pool> pool_;
@@ -1013,19 +1028,16 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
 // ordered commit (InscyNodeCpu.cu:159-235)
 // ---------------------------------------------------------------------------
 void Engine::replay(int ci) {
-  // copy what is needed: calls_ may not grow here, but keep indices stable
   const int f = calls_[ci].f;
   const uint64_t rmask = calls_[ci].rmask;
   const int depth = __builtin_popcountll(rmask);
   std::vector<int>& V = vbuf_[depth];
   if (V.empty()) V.assign(n_, -1);
-  std::vector<int> touched;
   size_t ri = 0;
   const size_t nreg = calls_[ci].regions.size();
   for (int D = f; D < d_; ++D) {
     const uint64_t smask = rmask | (1ull << D);
-    int nlabels = 0;
-    touched.clear();
+    LoopState st;
     while (ri < nreg && calls_[ci].regions[ri].dim == D) {
       const HRegion R = calls_[ci].regions[ri++];
       if (!R.passed) continue;
@@ -1033,15 +1045,21 @@ void Engine::replay(int ci) {
       auto t0 = std::chrono::steady_clock::now();
       bool ok = prune_redundancy(calls_[R.child], smask);
       auto t1 = std::chrono::steady_clock::now();
-      if (ok) cluster_into(calls_[R.child], V, touched, nlabels);
+      if (ok) cluster_into(calls_[R.child], V, st);
       auto t2 = std::chrono::steady_clock::now();
       t_prune_ += std::chrono::duration<double, std::milli>(t1 - t0).count();
       t_cluster_ += std::chrono::duration<double, std::milli>(t2 - t1).count();
     }
     auto t3 = std::chrono::steady_clock::now();
-    join(V, touched, nlabels, smask);
+    join(V, st, smask);
+    // clear the loop's vector through the numbered components
+    for (int l = 1; l <= st.nlabels; ++l) {
+      const HSub& hs = subs_[st.ref[l].csub];
+      const int c = st.ref[l].comp;
+      for (long long k = hs.moff[c]; k < hs.moff[c + 1]; ++k) V[hs.members[k]] = -1;
+      for (long long k = hs.boff[c]; k < hs.boff[c + 1]; ++k) V[hs.borders[k]] = -1;
+    }
     t_join_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t3).count();
-    for (int p : touched) V[p] = -1;
   }
 }
 
@@ -1100,11 +1118,15 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
       refresh_order(E);
       for (int l : E.by_size) {
         bool hit = false;
-        for (int q : E.mem[l])
+        const HSub& hs = subs_[E.src[l].csub];
+        const int cp = E.src[l].comp;
+        for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+          int q = hs.members[k];
           if (E.lab[q] == l && ((tbits_[q >> 6] >> (q & 63)) & 1ull)) {
             hit = true;
             break;
           }
+        }
         if (hit) {
           mn = E.size[l];
           break;
@@ -1127,7 +1149,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
 // BFS numbering of INSCYClusteringImplCPUAll (ClusteringCpu.cu:317-389):
 // components in the order their first dense seed appears, members get the
 // next label, non-dense neighbours that are still -1 become -2.
-void Engine::cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>& touched, int& nlabels) {
+void Engine::cluster_into(const HCall& c, std::vector<int>& V, LoopState& st) {
   const HSub& hs = subs_[c.csub];
   const int* order = levels_[c.level].order.data() + c.order_off;
   for (int t = 0; t < c.norder; ++t) {
@@ -1135,18 +1157,13 @@ void Engine::cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>&
     long long m0 = hs.moff[comp], m1 = hs.moff[comp + 1];
     if (m1 == m0) continue;
     if (V[hs.members[m0]] != -1) continue;  // already numbered in this dim loop
-    int label = ++nlabels;
-    for (long long k = m0; k < m1; ++k) {
-      int p = hs.members[k];
-      V[p] = label;
-      touched.push_back(p);
-    }
+    int label = ++st.nlabels;
+    st.ref.push_back(LabelRef{c.csub, comp});
+    st.size.push_back((int)(m1 - m0));
+    for (long long k = m0; k < m1; ++k) V[hs.members[k]] = label;
     for (long long k = hs.boff[comp]; k < hs.boff[comp + 1]; ++k) {
       int q = hs.borders[k];
-      if (V[q] == -1) {
-        V[q] = -2;
-        touched.push_back(q);
-      }
+      if (V[q] == -1) V[q] = -2;
     }
   }
 }
@@ -1154,26 +1171,30 @@ void Engine::cluster_into(const HCall& c, std::vector<int>& V, std::vector<int>&
 // join (util.cu:655-743): drop clusters below min_size, drop clusters a
 // superset subspace already covers with a cluster more than r times larger,
 // then insert the clustering or merge it into the subspace's entry (new
-// labels offset by the old maximum + 1, -2 marks overwrite).
-void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, uint64_t smask) {
-  if (nlabels == 0) return;
-  std::vector<int> sizes(nlabels + 1, 0);
-  for (int p : touched)
-    if (V[p] >= 0) sizes[V[p]]++;
+// labels offset by the old maximum + 1, -2 marks overwrite).  Works on whole
+// clusters: the loop's labels are components with known sizes.
+void Engine::join(std::vector<int>& V, LoopState& st, uint64_t smask) {
+  const int nl = st.nlabels;
+  if (nl == 0) return;
+  std::vector<char> alive(nl + 1, 0);
   int minsz = INT32_MAX;
-  for (int p : touched)
-    if (V[p] >= 0) {
-      if (sizes[V[p]] < hp_.min_size)
-        V[p] = -1;
-      else
-        minsz = std::min(minsz, sizes[V[p]]);
+  for (int l = 1; l <= nl; ++l)
+    if (st.size[l] >= hp_.min_size) {
+      alive[l] = 1;
+      minsz = std::min(minsz, st.size[l]);
     }
   if (minsz == INT32_MAX) return;
-  std::vector<char> drop(nlabels + 1, 0);
   for (int i : superset_candidates(smask)) {
     if ((emask_[i] & smask) != smask) continue;
     Entry& H = *ents_[i];
     bool hit = false;
+    auto test = [&](int q, int hsz) {
+      int c = V[q];
+      if (c > 0 && alive[c] && (float)st.size[c] * hp_.r < (float)hsz) {
+        alive[c] = 0;
+        hit = true;
+      }
+    };
     if (hp_.r >= 0.f) {
       // only clusters of H larger than (smallest cluster here) * r can drop
       // anything; walk them largest first (float comparisons as the reference)
@@ -1181,34 +1202,31 @@ void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, u
       refresh_order(H);
       for (int t = (int)H.by_size.size() - 1; t >= 0; --t) {
         const int l = H.by_size[t];
-        const int hs = H.size[l];
-        if (!((float)minsz * hp_.r < (float)hs)) break;
-        for (int q : H.mem[l]) {
-          if (H.lab[q] != l) continue;
-          int c = V[q];
-          if (c >= 0 && (float)sizes[c] * hp_.r < (float)hs) {
-            drop[c] = 1;
-            hit = true;
-          }
+        const int hsz = H.size[l];
+        if (!((float)minsz * hp_.r < (float)hsz)) break;
+        const HSub& hs = subs_[H.src[l].csub];
+        const int cp = H.src[l].comp;
+        for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+          int q = hs.members[k];
+          if (H.lab[q] == l) test(q, hsz);
         }
       }
     } else {
-      for (int p : touched) {
-        int c = V[p];
-        if (c < 0) continue;
-        int h = H.lab[p];
-        if (h >= 0 && (float)sizes[c] * hp_.r < (float)H.size[h]) {
-          drop[c] = 1;
-          hit = true;
+      for (int l = 1; l <= nl; ++l) {
+        if (!alive[l]) continue;
+        const HSub& hs = subs_[st.ref[l].csub];
+        const int cp = st.ref[l].comp;
+        for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+          int q = hs.members[k];
+          int h = H.lab[q];
+          if (h >= 0) test(q, H.size[h]);
         }
       }
     }
     if (hit) {
-      for (int p : touched)
-        if (V[p] >= 0 && drop[V[p]]) V[p] = -1;
       minsz = INT32_MAX;
-      for (int p : touched)
-        if (V[p] >= 0) minsz = std::min(minsz, sizes[V[p]]);
+      for (int l = 1; l <= nl; ++l)
+        if (alive[l]) minsz = std::min(minsz, st.size[l]);
       if (minsz == INT32_MAX) return;
     }
   }
@@ -1229,20 +1247,30 @@ void Engine::join(std::vector<int>& V, std::vector<int>& touched, int nlabels, u
     emask_.push_back(smask);
     off = 0;
   }
-  for (int p : touched) {
-    int v = V[p];
-    if (v == -1) continue;
-    int nv = v == -2 ? -2 : off + v;
-    int ov = E->lab[p];
-    if (ov >= 0) E->size[ov]--;
-    E->lab[p] = nv;
-    if (nv >= 0) {
-      if ((int)E->size.size() <= nv) {
-        E->size.resize(nv + 1, 0);
-        E->mem.resize(nv + 1);
+  const int top = off + nl;
+  if ((int)E->size.size() <= top) {
+    E->size.resize(top + 1, 0);
+    E->src.resize(top + 1, LabelRef{-1, -1});
+  }
+  for (int l = 1; l <= nl; ++l) {
+    const HSub& hs = subs_[st.ref[l].csub];
+    const int cp = st.ref[l].comp;
+    if (alive[l]) {
+      const int nv = off + l;
+      for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+        int p = hs.members[k];
+        int ov = E->lab[p];
+        if (ov >= 0) E->size[ov]--;
+        E->lab[p] = nv;
       }
-      E->size[nv]++;
-      E->mem[nv].push_back(p);
+      E->size[nv] += st.size[l];
+      E->src[nv] = st.ref[l];
+    }
+    for (long long k = hs.boff[cp]; k < hs.boff[cp + 1]; ++k) {
+      int q = hs.borders[k];
+      int ov = E->lab[q];
+      if (ov >= 0) E->size[ov]--;
+      E->lab[q] = -2;
     }
   }
   // v_max over the whole vector: the largest label that still has points,

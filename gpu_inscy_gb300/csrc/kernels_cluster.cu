@@ -63,8 +63,8 @@ __device__ __forceinline__ int uf_find(int* par, int x) {
   return cur;
 }
 
-__device__ __forceinline__ void uf_unite(int* par, int a, int b, int* err) {
-  int ra = uf_find(par, a), rb = uf_find(par, b);
+// unite the trees of roots-or-nodes ra and rb
+__device__ __forceinline__ void uf_unite(int* par, int ra, int rb, int* err) {
   int it = 0;
   while (ra != rb) {
     if (ra < rb) {
@@ -88,7 +88,8 @@ __global__ void k_uf_init(int* par, long long n) {
   if (i < n) par[i] = (int)i;
 }
 
-// one warp per kept point of a clustered subspace
+// one warp per kept point of a clustered subspace; its own root is found once
+// per 32 neighbours and only neighbours in another tree are united
 __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a) {
   const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (kk >= a.nkeep) return;
@@ -99,11 +100,25 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a) {
   if (!bit_of(dn, p)) return;
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
-  for (int j = lane_id(); j < len; j += 32) {
-    int q = a.lids[b + j];
-    if (!bit_of(dn, q)) continue;
-    long long kq = keep_index(a, si, q);
-    if (kq < kk) uf_unite(a.uf, (int)kk, (int)kq, a.err);
+  const unsigned lane = lane_id();
+  for (int j0 = 0; j0 < len; j0 += 32) {
+    const int j = j0 + (int)lane;
+    int kq = -1;
+    if (j < len) {
+      int q = a.lids[b + j];
+      if (bit_of(dn, q)) {
+        long long k2 = keep_index(a, si, q);
+        if (k2 < kk) kq = (int)k2;  // each edge once, from its larger end
+      }
+    }
+    if (!__any_sync(0xffffffffu, kq >= 0)) continue;
+    int rk = 0;
+    if (lane == 0) rk = uf_find(a.uf, (int)kk);
+    rk = __shfl_sync(0xffffffffu, rk, 0);
+    if (kq >= 0) {
+      int rq = uf_find(a.uf, kq);
+      if (rq != rk) uf_unite(a.uf, rk, rq, a.err);
+    }
   }
 }
 
