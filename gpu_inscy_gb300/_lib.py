@@ -22,8 +22,8 @@ MODE_BATCHED = 1
 
 # every symbol include/inscy_gb300.h declares
 EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_result_count", "inscy_result_n",
-           "inscy_result_subspace", "inscy_result_labels", "inscy_result_stats", "inscy_result_free",
-           "inscy_last_error", "inscy_version"]
+           "inscy_result_subspace", "inscy_result_labels", "inscy_result_labels_ptr", "inscy_result_stats",
+           "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest"]
 
 
 class Params(ctypes.Structure):
@@ -72,6 +72,10 @@ def load():
     lib.inscy_result_n.restype = i64
     lib.inscy_result_subspace.argtypes = [vp, c_int, vp, c_int]
     lib.inscy_result_labels.argtypes = [vp, c_int, vp]
+    lib.inscy_result_labels_ptr.argtypes = [vp, c_int]
+    lib.inscy_result_labels_ptr.restype = vp
+    lib.inscy_selftest.argtypes = [i64]
+    lib.inscy_selftest.restype = i64
     lib.inscy_result_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.inscy_result_free.argtypes = [vp]
     lib.inscy_result_free.restype = None
@@ -91,26 +95,46 @@ def check(rc):
         raise InscyError(rc, load().inscy_last_error().decode())
 
 
-def collect(handle, free=True):
-    """Turn a result handle into (subspaces: list[list[int]], labels: int32 [k, n], stats)."""
+class _Owner:
+    """Frees a result handle once no label view refers to it any more."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def __del__(self):
+        if self.handle and _lib is not None:
+            _lib.inscy_result_free(self.handle)
+            self.handle = None
+
+
+class _View:
+    """numpy view of one label vector inside a result (no copy)."""
+
+    def __init__(self, owner, ptr, n):
+        self.owner = owner
+        self.__array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, True), "version": 3}
+
+
+def collect(handle):
+    """Turn a result handle into (subspaces: list[list[int]], labels, stats).
+
+    `labels` is a list of int32 arrays of length n, one per clustered
+    subspace, viewing the result's memory (freed when the last view dies).
+    """
     lib = load()
-    try:
-        k = lib.inscy_result_count(handle)
-        n = lib.inscy_result_n(handle)
-        dims = np.zeros(64, np.int32)
-        subspaces = []
-        labels = np.empty((k, n), np.int32)
-        for i in range(k):
-            m = lib.inscy_result_subspace(handle, i, dims.ctypes.data, 64)
-            subspaces.append([int(x) for x in dims[:m]])
-            if n:
-                check(lib.inscy_result_labels(handle, i, labels[i].ctypes.data))
-        st = Stats()
-        check(lib.inscy_result_stats(handle, ctypes.byref(st)))
-        return subspaces, labels, st.as_dict()
-    finally:
-        if free:
-            lib.inscy_result_free(handle)
+    owner = _Owner(handle)
+    k = lib.inscy_result_count(handle)
+    n = lib.inscy_result_n(handle)
+    dims = np.zeros(64, np.int32)
+    subspaces, labels = [], []
+    for i in range(k):
+        m = lib.inscy_result_subspace(handle, i, dims.ctypes.data, 64)
+        subspaces.append([int(x) for x in dims[:m]])
+        ptr = lib.inscy_result_labels_ptr(handle, i)
+        labels.append(np.asarray(_View(owner, ptr, n)) if n else np.empty(0, np.int32))
+    st = Stats()
+    check(lib.inscy_result_stats(handle, ctypes.byref(st)))
+    return subspaces, labels, st.as_dict()
 
 
 def run_host(X, params, mode=MODE_PLAIN):

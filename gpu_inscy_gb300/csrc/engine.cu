@@ -232,6 +232,32 @@ struct Entry {
   bool dirty = true;
 };
 
+// The clustering vector of one dim loop (InscyNodeCpu.cu:175): n labels,
+// -1 by default.  A generation stamp per point makes clearing it O(1).
+struct LoopVec {
+  std::vector<int> val;
+  std::vector<unsigned> gen;
+  unsigned cur = 1;
+  void init(long long n) {
+    if ((long long)val.size() != n) {
+      val.assign(n, -1);
+      gen.assign(n, 0);
+      cur = 1;
+    }
+  }
+  void clear() {
+    if (++cur == 0) {  // wrapped: reset the stamps
+      std::fill(gen.begin(), gen.end(), 0u);
+      cur = 1;
+    }
+  }
+  int get(int p) const { return gen[p] == cur ? val[p] : -1; }
+  void set(int p, int v) {
+    gen[p] = cur;
+    val[p] = v;
+  }
+};
+
 // The clusters numbered in one dim loop (the reference's shared clustering
 // vector): label l -> component, and its size.
 struct LoopState {
@@ -309,8 +335,8 @@ class Engine {
   void replay(int ci);
   bool prune_redundancy(const HCall& c, uint64_t smask);
   const std::vector<int>& superset_candidates(uint64_t smask);
-  void cluster_into(const HCall& c, std::vector<int>& V, LoopState& st);
-  void join(std::vector<int>& V, LoopState& st, uint64_t smask);
+  void cluster_into(const HCall& c, LoopVec& V, LoopState& st);
+  void join(LoopVec& V, LoopState& st, uint64_t smask);
 
   int device_ = 0;
   std::unique_ptr<Pool> pool_;
@@ -329,7 +355,7 @@ class Engine {
   std::map<uint64_t, int> eidx_;              // subspace -> entry
   std::vector<std::vector<int>> by_dim_;      // entries whose subspace holds each dim
   std::vector<uint64_t> tbits_;               // region bitmap scratch
-  std::vector<std::vector<int>> vbuf_;        // one n-vector of labels per recursion depth
+  std::vector<LoopVec> vbuf_;                  // one clustering vector per recursion depth
   double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
   inscy_stats stats_;
 };
@@ -386,6 +412,24 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     float t = thr_weak;
     for (int j = k; j <= d; ++j) t = std::min(t, thr_dense[j]);
     thr_keep[k] = t;
+  }
+
+  // eps >= sqrtf(acc) (ClusteringCpu.cu:72) holds exactly for acc <= acc_max:
+  // correctly rounded sqrt is monotone, so the passing accs are a prefix of
+  // the non-negative floats; find its last element by bisection on the bits
+  float acc_max;
+  {
+    uint32_t lo = 0, hi = 0x7f800000u;  // [0, +inf)
+    while (lo < hi) {
+      uint32_t mid = lo + (hi - lo + 1) / 2;
+      float x;
+      std::memcpy(&x, &mid, 4);
+      if (hp.eps >= std::sqrt(x))
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    std::memcpy(&acc_max, &lo, 4);
   }
 
   Scope persist(*pool_, s);
@@ -598,6 +642,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.G = G;
     DL.eps = hp.eps;
     DL.rect = hp.rect;
+    DL.acc_max = acc_max;
     DL.thr_weak = thr_weak;
     DL.thr_dense = dthr;
     DL.thr_keep = dthr + d + 2;
@@ -612,24 +657,36 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.flags = dflags;
     DL.bitmaps = dbm;
     DL.words = W;
-    unsigned long long* dcand_cnt = lv.get<unsigned long long>(1);
-    CK(cudaMemsetAsync(dcand_cnt, 0, sizeof(unsigned long long), s));
+    unsigned long long* dcand_cnt = lv.get<unsigned long long>(2);
+    CK(cudaMemsetAsync(dcand_cnt, 0, 2 * sizeof(unsigned long long), s));
     DL.cand_counter = dcand_cnt;
-    double ms1 = timed(s, [&] { launch_neighbours(DL, false, s); });
+    DL.list_counter = dcand_cnt + 1;
+    long long ngroup_warps = 0;
+    for (auto& g : groups) ngroup_warps += g.nquery;
+    auto neighbours = [&](bool write) {
+      if (level == 1)
+        launch_neighbours(DL, write, s);
+      else
+        launch_neighbours_multi(DL, ngroup_warps, write, s);
+    };
+    double ms1 = timed(s, [&] { neighbours(false); });
     stats_.ms_density += ms1;
     stats_.ms_density_pass1 += ms1;
     stats_.density_launches_pass1 += 1;
     ++launches;
     {
-      // algorithmic bytes of the count pass: per query point 26 B (its id,
-      // list offset and length, own coordinate and fine cell, count out); per
-      // candidate 8 B at level 1 (id + coordinate) and 13 B above (id, stored
-      // partial distance, coordinate, fine cell)
-      unsigned long long nc = scalar(dcand_cnt, s);
-      stats_.candidates += (long long)nc;
-      stats_.density_bytes += 26.0 * (double)nitems + (level == 1 ? 8.0 : 13.0) * (double)nc;
+      // algorithmic bytes of the count pass: per (subspace, point) 26 B (its
+      // id, list offset and length, own coordinate and fine cell, count out);
+      // per list entry read 8 B (id + partial distance; at level 1 id +
+      // coordinate); per further (candidate, child subspace) test at levels
+      // >= 2 5 B (the candidate's coordinate and fine cell on that dim)
+      unsigned long long nc[2];
+      d2h(nc, dcand_cnt, sizeof(nc), s);
+      stats_.candidates += (long long)nc[0];
+      stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] + (level == 1 ? 0.0 : 5.0 * (double)nc[0]);
     }
     DL.cand_counter = nullptr;
+    DL.list_counter = nullptr;
 
     // ---- 3. ordered lists of every item, then densities and flags
     long long* dloff = lv.get<long long>(nitems);
@@ -644,7 +701,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.lids = lids;
     DL.lacc = lacc;
     stats_.ms_density += timed(s, [&] {
-      launch_neighbours(DL, true, s);
+      neighbours(true);
       launch_density_flags(DL, s);
     });
     launches += 2;
@@ -999,7 +1056,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
 
   // ---------------------------------------------------------------- commit
   auto t_rep0 = std::chrono::steady_clock::now();
-  vbuf_.assign(d + 2, std::vector<int>());
+  vbuf_.assign(d + 2, LoopVec());
   tbits_.assign(((size_t)n + 63) / 64, 0);
   t_prune_ = t_cluster_ = t_join_ = 0;
   replay(0);
@@ -1031,13 +1088,14 @@ void Engine::replay(int ci) {
   const int f = calls_[ci].f;
   const uint64_t rmask = calls_[ci].rmask;
   const int depth = __builtin_popcountll(rmask);
-  std::vector<int>& V = vbuf_[depth];
-  if (V.empty()) V.assign(n_, -1);
+  LoopVec& V = vbuf_[depth];
+  V.init(n_);
   size_t ri = 0;
   const size_t nreg = calls_[ci].regions.size();
   for (int D = f; D < d_; ++D) {
     const uint64_t smask = rmask | (1ull << D);
     LoopState st;
+    V.clear();
     while (ri < nreg && calls_[ci].regions[ri].dim == D) {
       const HRegion R = calls_[ci].regions[ri++];
       if (!R.passed) continue;
@@ -1052,13 +1110,6 @@ void Engine::replay(int ci) {
     }
     auto t3 = std::chrono::steady_clock::now();
     join(V, st, smask);
-    // clear the loop's vector through the numbered components
-    for (int l = 1; l <= st.nlabels; ++l) {
-      const HSub& hs = subs_[st.ref[l].csub];
-      const int c = st.ref[l].comp;
-      for (long long k = hs.moff[c]; k < hs.moff[c + 1]; ++k) V[hs.members[k]] = -1;
-      for (long long k = hs.boff[c]; k < hs.boff[c + 1]; ++k) V[hs.borders[k]] = -1;
-    }
     t_join_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t3).count();
   }
 }
@@ -1149,21 +1200,21 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
 // BFS numbering of INSCYClusteringImplCPUAll (ClusteringCpu.cu:317-389):
 // components in the order their first dense seed appears, members get the
 // next label, non-dense neighbours that are still -1 become -2.
-void Engine::cluster_into(const HCall& c, std::vector<int>& V, LoopState& st) {
+void Engine::cluster_into(const HCall& c, LoopVec& V, LoopState& st) {
   const HSub& hs = subs_[c.csub];
   const int* order = levels_[c.level].order.data() + c.order_off;
   for (int t = 0; t < c.norder; ++t) {
     int comp = order[t];
     long long m0 = hs.moff[comp], m1 = hs.moff[comp + 1];
     if (m1 == m0) continue;
-    if (V[hs.members[m0]] != -1) continue;  // already numbered in this dim loop
+    if (V.get(hs.members[m0]) != -1) continue;  // already numbered in this dim loop
     int label = ++st.nlabels;
     st.ref.push_back(LabelRef{c.csub, comp});
     st.size.push_back((int)(m1 - m0));
-    for (long long k = m0; k < m1; ++k) V[hs.members[k]] = label;
+    for (long long k = m0; k < m1; ++k) V.set(hs.members[k], label);
     for (long long k = hs.boff[comp]; k < hs.boff[comp + 1]; ++k) {
       int q = hs.borders[k];
-      if (V[q] == -1) V[q] = -2;
+      if (V.get(q) == -1) V.set(q, -2);
     }
   }
 }
@@ -1173,7 +1224,7 @@ void Engine::cluster_into(const HCall& c, std::vector<int>& V, LoopState& st) {
 // then insert the clustering or merge it into the subspace's entry (new
 // labels offset by the old maximum + 1, -2 marks overwrite).  Works on whole
 // clusters: the loop's labels are components with known sizes.
-void Engine::join(std::vector<int>& V, LoopState& st, uint64_t smask) {
+void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   const int nl = st.nlabels;
   if (nl == 0) return;
   std::vector<char> alive(nl + 1, 0);
@@ -1189,7 +1240,7 @@ void Engine::join(std::vector<int>& V, LoopState& st, uint64_t smask) {
     Entry& H = *ents_[i];
     bool hit = false;
     auto test = [&](int q, int hsz) {
-      int c = V[q];
+      int c = V.get(q);
       if (c > 0 && alive[c] && (float)st.size[c] * hp_.r < (float)hsz) {
         alive[c] = 0;
         hit = true;
@@ -1424,5 +1475,28 @@ void inscy_result_free(inscy_result* r) { delete r; }
 const char* inscy_last_error(void) { return g_err.c_str(); }
 
 const char* inscy_version(void) { return "inscy_gb300 0.1"; }
+
+int64_t inscy_selftest(int64_t count) {
+  try {
+    unsigned long long* d = nullptr;
+    CK(cudaMalloc(&d, sizeof(unsigned long long)));
+    CK(cudaMemset(d, 0, sizeof(unsigned long long)));
+    inscy::launch_phi_selftest((unsigned long long)count, 0x5eedull, d, 0);
+    CK(cudaGetLastError());
+    unsigned long long bad = 0;
+    CK(cudaMemcpy(&bad, d, sizeof(bad), cudaMemcpyDeviceToHost));
+    cudaFree(d);
+    g_err.clear();
+    return (int64_t)bad;
+  } catch (const inscy::Error& e) {
+    fail(e.code, e.what());
+    return -1;
+  }
+}
+
+const int32_t* inscy_result_labels_ptr(const inscy_result* r, int i) {
+  if (!r || i < 0 || i >= (int)r->labels.size()) return nullptr;
+  return r->labels[i].data();
+}
 
 }  // extern "C"

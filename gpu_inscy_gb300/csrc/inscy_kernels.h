@@ -36,6 +36,7 @@ struct DensityLaunch {
   int n, d, G;
   float eps;
   int rect;
+  float acc_max;
   float thr_weak;
   const float* thr_dense;
   const float* thr_keep;
@@ -54,9 +55,12 @@ struct DensityLaunch {
   int* lids;
   float* lacc;
   unsigned long long* cand_counter;
+  unsigned long long* list_counter;
 };
 void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s);
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s);
+void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
+void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s);
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
                         cudaStream_t s);
 void launch_keep_compact(const SubDesc* subs, int nsubs, long long nitems, const uint8_t* flags, const int* cnt,

@@ -23,6 +23,7 @@
 
 #include "inscy_common.cuh"
 #include "inscy_kernels.h"
+#include "phi_exact.cuh"
 
 namespace inscy {
 
@@ -38,6 +39,7 @@ struct DensityArgs {
   int n, d, G;
   float eps;
   int rect;
+  float acc_max;  // eps >= sqrt(acc)  <=>  acc <= acc_max (sqrt is monotone)
   float thr_weak;
   const float* thr_dense;  // [|S|]
   const float* thr_keep;   // [|S|]
@@ -58,7 +60,8 @@ struct DensityArgs {
   const long long* loff;  // [nitems] list start of every item
   int* lids;
   float* lacc;
-  unsigned long long* cand_counter;  // candidates tested
+  unsigned long long* cand_counter;  // candidate tests (candidate x child subspace)
+  unsigned long long* list_counter;  // list entries read
 };
 
 __device__ __forceinline__ int find_sub(const SubDesc* subs, int nsubs, long long item) {
@@ -135,7 +138,7 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     if (ok) {
       float acc = level1 ? 0.f : accs[j];
       acc2 = dist_step(acc, xp, a.X[(size_t)q * a.d + D]);
-      ok = a.eps >= __fsqrt_rn(acc2);
+      ok = acc2 <= a.acc_max;
     }
     unsigned m = __ballot_sync(0xffffffffu, ok);
     if (kWrite && ok) {
@@ -148,6 +151,86 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
   if (!kWrite && lane == 0) {
     a.cnt[item] = count;
     if (a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len);
+    if (a.list_counter) atomicAdd(a.list_counter, (unsigned long long)len);
+  }
+}
+
+// Levels >= 2: every child subspace of a parent filters the same parent list
+// of p, so one warp per (parent, p) reads that list once and tests each
+// candidate against all children (the candidate's row of X and of the fine
+// cells is loaded once).  Lane c keeps the running count of child c (and
+// c + 32).
+template <bool kWrite>
+__global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= a.nwarps) return;
+  const unsigned lane = lane_id();
+  int lo = 0, hi = a.ngroups - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.groups[mid].warp_off <= w)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const GroupDesc g = a.groups[lo];
+  const long long i = w - g.warp_off;
+  const int nc = g.nchild;
+  const SubDesc& S0 = a.subs[g.sub_base];
+  const int p = a.prev_keep[S0.query_off + i];
+  const long long pb = a.prev_loff[S0.query_off + i];
+  const int* ids = a.prev_lids + pb;
+  const float* accs = a.prev_lacc + pb;
+  const long long len = a.prev_lcnt[S0.query_off + i];
+  const float* xrow_p = a.X + (size_t)p * a.d;
+  const uint8_t* frow_p = a.fc + (size_t)p * a.d;
+  int run0 = 0, run1 = 0;  // lane c: children c and c + 32
+  long long ob0 = 0, ob1 = 0;
+  if (kWrite) {
+    if ((int)lane < nc) ob0 = a.loff[a.subs[g.sub_base + lane].item_off + i];
+    if ((int)lane + 32 < nc) ob1 = a.loff[a.subs[g.sub_base + lane + 32].item_off + i];
+  }
+  for (long long j0 = 0; j0 < len; j0 += 32) {
+    const long long j = j0 + lane;
+    const bool in = j < len;
+    const int q = in ? ids[j] : p;
+    const float acc = in ? accs[j] : 0.f;
+    const float* xrow_q = a.X + (size_t)q * a.d;
+    const uint8_t* frow_q = a.fc + (size_t)q * a.d;
+    for (int c = 0; c < nc; ++c) {
+      const int D = a.subs[g.sub_base + c].dim;
+      const int fp = frow_p[D];
+      const int fq = frow_q[D];
+      bool ok = in && q != p && fq >= fp - 1 && fq <= fp + 1;
+      float acc2 = 0.f;
+      if (ok) {
+        acc2 = dist_step(acc, xrow_p[D], xrow_q[D]);
+        ok = acc2 <= a.acc_max;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, ok);
+      if (!m) continue;
+      if (kWrite) {
+        const int owner = c & 31;
+        long long base = __shfl_sync(0xffffffffu, c < 32 ? ob0 + run0 : ob1 + run1, owner);
+        if (ok) {
+          long long o = base + __popc(m & lanemask_lt());
+          a.lids[o] = q;
+          a.lacc[o] = acc2;
+        }
+      }
+      if ((int)lane == (c & 31)) {
+        if (c < 32)
+          run0 += __popc(m);
+        else
+          run1 += __popc(m);
+      }
+    }
+  }
+  if (!kWrite) {
+    if ((int)lane < nc) a.cnt[a.subs[g.sub_base + lane].item_off + i] = run0;
+    if ((int)lane + 32 < nc) a.cnt[a.subs[g.sub_base + lane + 32].item_off + i] = run1;
+    if (lane == 0 && a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len * nc);
+    if (lane == 0 && a.list_counter) atomicAdd(a.list_counter, (unsigned long long)len);
   }
 }
 
@@ -167,7 +250,10 @@ __global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
   } else {
     const float* acc = a.lacc + a.loff[item];
     float sum = 0.f;
-    for (int j = 0; j < c; ++j) sum = phi_add(sum, phi_term(__fsqrt_rn(acc[j]), a.eps));
+    for (int j = 0; j < c; ++j) {
+      const float dd = __fdiv_rn(__fsqrt_rn(acc[j]), a.eps);
+      sum = phi_step_exact(sum, __fmul_rn(dd, dd));
+    }
     v = sum;
   }
   uint8_t f = 0;
@@ -277,6 +363,7 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.G = L.G;
   a.eps = L.eps;
   a.rect = L.rect;
+  a.acc_max = L.acc_max;
   a.thr_weak = L.thr_weak;
   a.thr_dense = L.thr_dense;
   a.thr_keep = L.thr_keep;
@@ -295,6 +382,7 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.lids = L.lids;
   a.lacc = L.lacc;
   a.cand_counter = L.cand_counter;
+  a.list_counter = L.list_counter;
   return a;
 }
 
@@ -306,6 +394,52 @@ void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s) {
     k_neighbours<true><<<blocks, 256, 0, s>>>(a);
   else
     k_neighbours<false><<<blocks, 256, 0, s>>>(a);
+}
+
+// self-test: the integer phi step against the double-precision expression on
+// pseudo-random and edge inputs; counts mismatches
+__global__ void k_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long x = (i + 1) * 0x9e3779b97f4a7c15ull ^ seed;
+  x ^= x >> 31;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  float sum;
+  const int mode = (int)(x & 3);
+  if (mode == 0)
+    sum = (float)((x >> 8) % 100000);
+  else if (mode == 1)
+    sum = 0.f;
+  else
+    sum = __uint_as_float(((uint32_t)((int)((x >> 40) % 42) - 24 + 127) << 23) | ((uint32_t)(x >> 8) & 0x7fffffu));
+  unsigned long long y = x * 0x94d049bb133111ebull;
+  y ^= y >> 29;
+  float sq;
+  if (y & 1)
+    sq = __uint_as_float((uint32_t)(y >> 8) % 0x3f800001u);
+  else {
+    float dd = (float)((y >> 11) * 0x1p-53);
+    sq = __fmul_rn(dd, dd);
+  }
+  if (sq > 1.f) sq = 1.f;
+  if (__float_as_uint(phi_step_exact(sum, sq)) != __float_as_uint(phi_step_double(sum, sq))) atomicAdd(bad, 1ull);
+}
+
+void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s) {
+  k_phi_selftest<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, seed, bad);
+}
+
+// level >= 2: one warp per (parent group, query point)
+void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s) {
+  if (nwarps <= 0) return;
+  DensityArgs a = make_args(L);
+  a.nwarps = nwarps;
+  unsigned blocks = (unsigned)((nwarps * 32 + 255) / 256);
+  if (write)
+    k_neighbours_multi<true><<<blocks, 256, 0, s>>>(a);
+  else
+    k_neighbours_multi<false><<<blocks, 256, 0, s>>>(a);
 }
 
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s) {

@@ -38,16 +38,19 @@ def _run(X, neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectang
             stream = torch.cuda.current_stream(Xc.device).cuda_stream
             with torch.cuda.device(Xc.device):
                 subs, labels, stats = _lib.run_device(Xc.data_ptr(), Xc.shape[0], Xc.shape[1], p, stream, mode)
-            return (subs, labels) if as_numpy else (subs, labels.tolist())
+            return (subs, labels) if as_numpy else (subs, [l.tolist() for l in labels])
     except ImportError:  # pragma: no cover
         pass
     subs, labels, stats = _lib.run_host(_as_numpy(X), p, mode)
-    return (subs, labels) if as_numpy else (subs, labels.tolist())
+    return (subs, labels) if as_numpy else (subs, [l.tolist() for l in labels])
 
 
 def GPU(X, neighborhood_size, F, num_obj, min_size, r=1., number_of_cells=3, rectangular=False, entropy_order=0,
         as_numpy=False):
-    """Plain GPU INSCY (replaces python/inscy.py:189 GPU -> run_gpu_4)."""
+    """Plain GPU INSCY (replaces python/inscy.py:189 GPU -> run_gpu_4).
+
+    Returns (subspaces, clusterings) as Python lists like the reference; with
+    as_numpy=True the clusterings are a list of int32 arrays (no copy)."""
     return _run(X, neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectangular, entropy_order,
                 _lib.MODE_PLAIN, as_numpy)
 

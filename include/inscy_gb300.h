@@ -103,6 +103,7 @@ int inscy_result_count(const inscy_result* r);              /* number of cluster
 int64_t inscy_result_n(const inscy_result* r);              /* number of points */
 int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap); /* returns |S|, writes min(|S|,cap) dims */
 int inscy_result_labels(const inscy_result* r, int i, int32_t* out);        /* copies n labels */
+const int32_t* inscy_result_labels_ptr(const inscy_result* r, int i);       /* n labels, valid until free; NULL on bad i */
 int inscy_result_stats(const inscy_result* r, inscy_stats* out);
 void inscy_result_free(inscy_result* r);
 
@@ -111,6 +112,12 @@ const char* inscy_last_error(void);
 
 /* Library version string. */
 const char* inscy_version(void);
+
+/* Device self-test: checks `count` pseudo-random and edge inputs of the
+ * integer form of the reference's phi accumulation step against the
+ * double-precision expression on the current GPU.  Returns the number of
+ * mismatches (0 expected), or -1 with inscy_last_error() set. */
+int64_t inscy_selftest(int64_t count);
 
 #ifdef __cplusplus
 }

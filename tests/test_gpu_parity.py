@@ -66,6 +66,22 @@ def test_plain_workload_shape_matches_oracle(engine):
     assert len(want[0]) > 0
 
 
+def test_phi_step_selftest(engine):
+    # the integer form of the reference's phi accumulation step vs the
+    # double-precision expression, on the GPU
+    assert engine.inscy_selftest(50_000_000) == 0
+
+
+def test_labels_are_views_that_outlive_the_call(engine):
+    X, p = _random_case(21)
+    (subs, labels), _ = gpu_run(X, **p)
+    want = orc.run(X, **p)
+    del X
+    import gc
+    gc.collect()
+    assert_same((subs, [l.copy() for l in labels]), want, "views")
+
+
 def test_batched_mode_equals_plain(engine):
     X, p = _random_case(101)
     a, _ = gpu_run(X, mode=_lib.MODE_PLAIN, **p)
@@ -111,7 +127,7 @@ BASE = dict(neighborhood_size=0.1, F=1.0, num_obj=2, min_size=3, r=1.0, number_o
 
 def test_empty_input(engine):
     (subs, labels), _ = gpu_run(np.zeros((0, 4), np.float32), **BASE)
-    assert subs == [] and labels.shape[0] == 0
+    assert subs == [] and len(labels) == 0
 
 
 def test_single_point(engine):
