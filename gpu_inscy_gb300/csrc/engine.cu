@@ -604,6 +604,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
 
     // groups: the children of one parent subspace, walked child-fastest
     std::vector<GroupDesc> groups;
+    long long ngroup_warps = 0;  // one warp per (group, query point)
     {
       long long wo = 0;
       for (int i = 0; i < nsubs;) {
@@ -611,14 +612,17 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         while (j < nsubs && subs[j].parent == subs[i].parent) ++j;
         GroupDesc g;
         g.warp_off = wo;
+        g.qwarp_off = ngroup_warps;
         g.sub_base = i;
         g.nchild = j - i;
         g.nquery = subs[i].nquery;
         g.pad = 0;
         wo += (long long)g.nchild * g.nquery;
+        ngroup_warps += g.nquery;
         groups.push_back(g);
         i = j;
       }
+      if (wo != nitems) throw Error(INSCY_ERR_INTERNAL, "work item count mismatch");
     }
     GroupDesc* dgroups = lv.get<GroupDesc>(groups.size());
     h2d(dgroups, groups.data(), sizeof(GroupDesc) * groups.size(), s);
@@ -661,8 +665,6 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     CK(cudaMemsetAsync(dcand_cnt, 0, 2 * sizeof(unsigned long long), s));
     DL.cand_counter = dcand_cnt;
     DL.list_counter = dcand_cnt + 1;
-    long long ngroup_warps = 0;
-    for (auto& g : groups) ngroup_warps += g.nquery;
     auto neighbours = [&](bool write) {
       if (level == 1)
         launch_neighbours(DL, write, s);

@@ -64,7 +64,8 @@ struct SubDesc {
 
 // The children of one parent subspace (contiguous subspace indices).
 struct GroupDesc {
-  long long warp_off;  // first work item (warp) of the group
+  long long warp_off;   // first (child, query) work item of the group
+  long long qwarp_off;  // first query of the group (one warp per query)
   int sub_base;
   int nchild;
   int nquery;

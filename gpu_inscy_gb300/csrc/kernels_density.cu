@@ -168,13 +168,14 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
   int lo = 0, hi = a.ngroups - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (a.groups[mid].warp_off <= w)
+    if (a.groups[mid].qwarp_off <= w)
       lo = mid;
     else
       hi = mid - 1;
   }
   const GroupDesc g = a.groups[lo];
-  const long long i = w - g.warp_off;
+  const long long i = w - g.qwarp_off;
+  if (i < 0 || i >= g.nquery) return;  // unreachable when the offsets are consistent
   const int nc = g.nchild;
   const SubDesc& S0 = a.subs[g.sub_base];
   const int p = a.prev_keep[S0.query_off + i];
