@@ -23,7 +23,7 @@ MODE_BATCHED = 1
 # every symbol include/inscy_gb300.h declares
 EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_result_count", "inscy_result_n",
            "inscy_result_subspace", "inscy_result_labels", "inscy_result_labels_ptr", "inscy_result_stats",
-           "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest"]
+           "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest", "inscy_selftest_noalloc"]
 
 
 class Params(ctypes.Structure):
@@ -76,6 +76,8 @@ def load():
     lib.inscy_result_labels_ptr.restype = vp
     lib.inscy_selftest.argtypes = [i64]
     lib.inscy_selftest.restype = i64
+    lib.inscy_selftest_noalloc.argtypes = [i64, vp]
+    lib.inscy_selftest_noalloc.restype = i64
     lib.inscy_result_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.inscy_result_free.argtypes = [vp]
     lib.inscy_result_free.restype = None

@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libinscy_gb300.so")
-SOURCES = ["engine.cu", "kernels_setup.cu", "kernels_density.cu", "kernels_tree.cu", "kernels_cluster.cu"]
+SOURCES = ["engine.cu", "kernels_setup.cu", "kernels_density.cu", "kernels_tree.cu", "kernels_cluster.cu",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-fmad=false",
          "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-Xptxas", "-v"]

@@ -119,6 +119,26 @@ const char* inscy_version(void);
  * mismatches (0 expected), or -1 with inscy_last_error() set. */
 int64_t inscy_selftest(int64_t count);
 
+/* inscy_selftest without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc while they check a
+ * GPU, e.g. a process whose device memory is already fully handed to a
+ * caching allocator or capped, or a latency-critical path that must avoid
+ * cudaMalloc's implicit synchronisation.  The only scratch, the mismatch
+ * counter, is a 256-byte file-scope device array inside the library (held on
+ * every GPU that loads it until exit).  The first call on a device looks up
+ * the array's device address, so make that first call before any stream
+ * capture.  Every call clears the counter; calls that overlap on the GPU
+ * share it and race.  Same result as inscy_selftest(count) (work queued on
+ * `stream`, a cudaStream_t or NULL).  count is limited to
+ * INSCY_SELFTEST_NOALLOC_MAX; returns the mismatch count (0 expected),
+ * INSCY_SELFTEST_NOALLOC_TOO_LARGE for count < 0 or above the limit, or
+ * INSCY_SELFTEST_NOALLOC_CUDA when a CUDA call fails.  It does not touch
+ * inscy_last_error(). */
+#define INSCY_SELFTEST_NOALLOC_MAX (1LL << 31)
+#define INSCY_SELFTEST_NOALLOC_TOO_LARGE (-1)
+#define INSCY_SELFTEST_NOALLOC_CUDA (-2)
+int64_t inscy_selftest_noalloc(int64_t count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
