@@ -243,6 +243,7 @@ def main():
                                                "ms_cluster", "ms_replay", "ms_replay_prune", "ms_replay_cluster",
                                                "ms_replay_join", "ms_d2h", "ms_total")},
             "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
+            "commit_counters": st["replay"],
             "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(X, p, args.cpu_sample)

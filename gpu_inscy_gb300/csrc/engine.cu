@@ -357,6 +357,7 @@ class Engine {
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<LoopVec> vbuf_;                  // one clustering vector per recursion depth
   double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
+  long long* rc_ = nullptr;  // stats_.replay_counters
   inscy_stats stats_;
 };
 
@@ -1061,6 +1062,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   vbuf_.assign(d + 2, LoopVec());
   tbits_.assign(((size_t)n + 63) / 64, 0);
   t_prune_ = t_cluster_ = t_join_ = 0;
+  rc_ = stats_.replay_counters;
   replay(0);
   stats_.ms_replay_prune = t_prune_;
   stats_.ms_replay_cluster = t_cluster_;
@@ -1149,6 +1151,7 @@ static void refresh_order(Entry& E) {
 bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
   const int* pts = levels_[c.level].pts.data() + c.pts_off;
   const int m = c.npts;
+  rc_[6]++;
   const double thr = (double)((float)m * hp_.r);
   const bool use_bits = (long long)m * 8 > n_;
   if (use_bits)
@@ -1160,6 +1163,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
     Entry& E = *ents_[i];
     int mn = -1;
     if (!use_bits) {
+      rc_[7] += m;
       for (int j = 0; j < m; ++j) {
         int l = E.lab[pts[j]];
         if (l >= 0) {
@@ -1175,6 +1179,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
         const int cp = E.src[l].comp;
         for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
           int q = hs.members[k];
+          rc_[7]++;
           if (E.lab[q] == l && ((tbits_[q >> 6] >> (q & 63)) & 1ull)) {
             hit = true;
             break;
@@ -1211,6 +1216,8 @@ void Engine::cluster_into(const HCall& c, LoopVec& V, LoopState& st) {
     if (m1 == m0) continue;
     if (V.get(hs.members[m0]) != -1) continue;  // already numbered in this dim loop
     int label = ++st.nlabels;
+    rc_[8]++;
+    rc_[9] += hs.boff[comp + 1] - hs.boff[comp];
     st.ref.push_back(LabelRef{c.csub, comp});
     st.size.push_back((int)(m1 - m0));
     for (long long k = m0; k < m1; ++k) V.set(hs.members[k], label);
@@ -1229,6 +1236,7 @@ void Engine::cluster_into(const HCall& c, LoopVec& V, LoopState& st) {
 void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   const int nl = st.nlabels;
   if (nl == 0) return;
+  rc_[0]++;
   std::vector<char> alive(nl + 1, 0);
   int minsz = INT32_MAX;
   for (int l = 1; l <= nl; ++l)
@@ -1240,8 +1248,10 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   for (int i : superset_candidates(smask)) {
     if ((emask_[i] & smask) != smask) continue;
     Entry& H = *ents_[i];
+    rc_[4]++;
     bool hit = false;
     auto test = [&](int q, int hsz) {
+      rc_[5]++;
       int c = V.get(q);
       if (c > 0 && alive[c] && (float)st.size[c] * hp_.r < (float)hsz) {
         alive[c] = 0;
@@ -1294,6 +1304,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     ne->mask = smask;
     ne->lab.assign(n_, -1);
     E = ne.get();
+    rc_[1]++;
     eidx_[smask] = (int)ents_.size();
     for (uint64_t m = smask; m; m &= m - 1) by_dim_[__builtin_ctzll(m)].push_back((int)ents_.size());
     ents_.push_back(std::move(ne));
@@ -1318,7 +1329,9 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       }
       E->size[nv] += st.size[l];
       E->src[nv] = st.ref[l];
+      rc_[2] += st.size[l];
     }
+    rc_[3] += hs.boff[cp + 1] - hs.boff[cp];
     for (long long k = hs.boff[cp]; k < hs.boff[cp + 1]; ++k) {
       int q = hs.borders[k];
       int ov = E->lab[q];

@@ -78,6 +78,11 @@ typedef struct inscy_stats {
   long long candidates;      /* candidate pairs tested */
   long long levels;
   long long h2d_bytes, d2h_bytes;
+  /* commit work counters: joins with clusters, new entries, label writes,
+   * border writes, superset entries examined by join, points visited by
+   * join's redundancy test, pruneRedundancy calls, points visited by
+   * pruneRedundancy, clusters numbered, border checks while numbering */
+  long long replay_counters[10];
 } inscy_stats;
 
 /* Replaces run_gpu_5 / run_gpu_4 (inscy_map.cpp:1070-1158 / :979-1067).
