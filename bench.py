@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-WORKLOAD = "plain_n25000_d15"
+WORKLOAD = "plain_n25000_d15"  # the default; --n changes n for profiling captures
 METRIC = "INSCY points/sec (plain GPU run, bit-exact labels)"
 
 
@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--n", type=int, default=25_000, help="points (profiling captures use a smaller case)")
     ap.add_argument("--cpu-sample", type=int, default=2000, help="rows of the workload the CPU baseline runs on")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the label check against the oracle")
@@ -147,7 +148,7 @@ def run_reference(args, X, p):
 def main():
     args = parse()
     from gpu_inscy_gb300 import synth
-    X = synth.make_plain(args.seed)
+    X = synth.make_plain(args.seed, n=args.n)
     p = dict(synth.PARAMS["plain"])
     if args.impl == "reference":
         run_reference(args, X, p)
