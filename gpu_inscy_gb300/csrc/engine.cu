@@ -459,6 +459,17 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   float* dthr = persist.get<float>(2 * (d + 2));
   h2d(dthr, thr_dense.data(), sizeof(float) * (d + 2), s);
   h2d(dthr + d + 2, thr_keep.data(), sizeof(float) * (d + 2), s);
+  // device-side consistency checks (code, offending value)
+  long long* dguard = persist.get<long long>(2);
+  CK(cudaMemsetAsync(dguard, 0, 2 * sizeof(long long), s));
+  Guard guard{(int*)dguard, dguard + 1};
+  auto check_guard = [&](const char* where) {
+    long long g[2];
+    d2h(g, dguard, sizeof(g), s);
+    if ((int)g[0] != 0)
+      throw Error(INSCY_ERR_INTERNAL, std::string("device check ") + std::to_string((int)g[0]) + " failed in " +
+                                          where + " (value " + std::to_string(g[1]) + ")");
+  };
   launch_prep(dX, ni, d, cells, csz, G, fsz, hp.eps, dcc, dfc, dgz, s);
   ++launches;
   int* drank = persist.get<int>(n);
@@ -553,7 +564,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     int* keep_lcnt = nullptr;
     int* lids = nullptr;
     float* lacc = nullptr;
+    long long total = 0;  // list entries
+    long long nkeep = 0;  // kept points
   } prev;
+  long long pts_in_total = n, ghosts_in_total = 0;
 
   int level = 0;
   while (!hcalls.empty()) {
@@ -662,6 +676,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.flags = dflags;
     DL.bitmaps = dbm;
     DL.words = W;
+    DL.prev_total = prev.total;
+    DL.prev_nkeep = prev.nkeep;
+    DL.total = 0;
+    DL.guard = guard;
     unsigned long long* dcand_cnt = lv.get<unsigned long long>(2);
     CK(cudaMemsetAsync(dcand_cnt, 0, 2 * sizeof(unsigned long long), s));
     DL.cand_counter = dcand_cnt;
@@ -703,6 +721,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     DL.loff = dloff;
     DL.lids = lids;
     DL.lacc = lacc;
+    DL.total = L;
     stats_.ms_density += timed(s, [&] {
       neighbours(true);
       launch_density_flags(DL, s);
@@ -716,6 +735,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     launch_exclusive_scan_i2ll(dkflag, dkpos, nitems, dtot + 1, sums, s);
     launches += 4;
     const long long K = scalar(dtot + 1, s);
+    check_guard("density");
     int* keep_ids = keepmem->get<int>(K);
     long long* keep_loff = keepmem->get<long long>(K);
     int* keep_lcnt = keepmem->get<int>(K);
@@ -807,6 +827,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       TL.out_ghost_top = dtops + 1;
       TL.out_ghost_cap = ghost_cap;
       TL.err = derr;
+      TL.pts_in_total = pts_in_total;
+      TL.ghosts_in_total = ghosts_in_total;
+      TL.guard = guard;
       stats_.ms_tree += timed(s, [&] { launch_tree_level(TL, s); });
       ++launches;
       int err = scalar(derr, s);
@@ -816,6 +839,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         continue;
       }
       if (err) throw Error(INSCY_ERR_INTERNAL, "level kernel reported error " + std::to_string(err));
+      check_guard("restrict/merge/prune");
       break;
     }
     recs.resize((size_t)nwork * cells);
@@ -918,21 +942,23 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       CA.n = ni;
       CA.uf = lv.get<int>(K + 1);
       CA.err = derr;
+      CA.guard = guard;
       CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
       int* is_root = lv.get<int>(K + 1);
       int* root_id = lv.get<int>(K + 1);
       int* comp = lv.get<int>(K + 1);
       int* root_of = lv.get<int>(K + 1);
+      int* dsample = lv.get<int>(ncl + 1);
       int* dnc = lv.get<int>(1);
       long long ncomp = 0;
       std::vector<int> cbase(nsubs + 1);
       stats_.ms_cluster += timed(s, [&] {
         launch_uf_init(CA.uf, K, s);
-        launch_uf_union(CA, s);
+        launch_uf_union(CA, ncl, dcslot, dsample, s);
         launch_uf_flatten(CA, is_root, root_of, s);
         launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
       });
-      launches += 6;
+      launches += 8;
       ncomp = scalar(dnc, s);
       int* dcbase = lv.get<int>(nsubs + 1);
       launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);
@@ -971,6 +997,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       launches += 1;
       hovf = scalar(novf, s);
       if (scalar(derr, s)) throw Error(INSCY_ERR_INTERNAL, "clustering kernels reported an error");
+      check_guard("clustering");
       hovf = std::min(hovf, ovf_cap);
       launch_border_count(slots, nslots2, ovf, hovf, bcount, s);
       launch_exclusive_scan_i2ll(bcount, boff, ncomp, dmtot + 1, sums, s);
@@ -1008,6 +1035,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       launches += 4;
       hl.order.resize(norder_tot);
       d2h(hl.order.data(), packed, sizeof(int) * norder_tot, s);
+      check_guard("component order");
       d2h(hocnt.data(), order_cnt, sizeof(int) * ncall.size(), s);
       std::vector<long long> hooff(ncall.size());
       d2h(hooff.data(), order_off, sizeof(long long) * ncall.size(), s);
@@ -1044,6 +1072,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     prev.keep_lcnt = keep_lcnt;
     prev.lids = lids;
     prev.lacc = lacc;
+    prev.total = L;
+    prev.nkeep = K;
+    pts_in_total = (long long)tops[0];
+    ghosts_in_total = (long long)tops[1];
     cur_pts = std::move(next_pts);
     d_pts = dout_pts;
     d_ghosts = dout_gh;

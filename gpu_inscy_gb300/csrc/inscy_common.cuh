@@ -72,6 +72,20 @@ struct GroupDesc {
   int pad;
 };
 
+// Device-side consistency checks: the first failed check records its code and
+// the offending value; the caller skips the access and the host reports the
+// failure after the launch (INSCY_ERR_INTERNAL) instead of touching memory out
+// of range.
+struct Guard {
+  int* code;
+  long long* info;
+};
+__device__ __forceinline__ bool guard_fail(const Guard& g, int code, long long v) {
+  if (atomicCAS(g.code, 0, code) == 0) *g.info = v;
+  return false;
+}
+#define GUARD_OK(g, cond, code, v) ((cond) || guard_fail((g), (code), (long long)(v)))
+
 // Per-point flag bits of a (subspace, point) evaluation.
 enum : uint8_t { kFlagWeak = 1, kFlagDense = 2, kFlagKeep = 4 };
 

@@ -56,6 +56,10 @@ struct DensityLaunch {
   float* lacc;
   unsigned long long* cand_counter;
   unsigned long long* list_counter;
+  long long prev_total;
+  long long total;
+  long long prev_nkeep;
+  Guard guard;
 };
 void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s);
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s);
@@ -98,6 +102,9 @@ struct TreeLaunch {
   unsigned long long* out_ghost_top;
   long long out_ghost_cap;
   int* err;
+  long long pts_in_total;
+  long long ghosts_in_total;
+  Guard guard;
 };
 void launch_tree_level(const TreeLaunch& L, cudaStream_t s);
 
@@ -119,9 +126,10 @@ struct ClusterArgs {
   int n;
   int* uf;
   int* err;
+  Guard guard;
 };
 void launch_uf_init(int* par, long long n, cudaStream_t s);
-void launch_uf_union(const ClusterArgs& a, cudaStream_t s);
+void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, cudaStream_t s);
 void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s);
 void launch_comp_ids(const ClusterArgs& a, const int* root_id, const int* root_of, int* comp, int* mcount,
                      cudaStream_t s);

@@ -88,9 +88,72 @@ __global__ void k_uf_init(int* par, long long n) {
   if (i < n) par[i] = (int)i;
 }
 
-// one warp per kept point of a clustered subspace; its own root is found once
-// per 32 neighbours and only neighbours in another tree are united
-__global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a) {
+// Connected components of the dense points of every clustered subspace, in
+// the Afforest order: (1) every dense point is united with its first two dense
+// neighbours; (2) per subspace, the component most of 32 sampled dense points
+// fall in is taken as the dominant one; (3) only points outside the dominant
+// component (checked when they are processed) unite with all their dense
+// neighbours.  Every edge that is skipped joins two points that were both in
+// the dominant component at some time, and components only grow, so the final
+// partition is the connected components of the full neighbour relation.
+
+// (1) one thread per kept point
+__global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  if (!a.clustered[si]) return;
+  const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+  if (!bit_of(dn, a.keep_ids[kk])) return;
+  const long long b = a.keep_loff[kk];
+  const int len = a.keep_lcnt[kk];
+  int linked = 0;
+  for (int j = 0; j < len && linked < 2; ++j) {
+    int q = a.lids[b + j];
+    if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 63, q) || !bit_of(dn, q)) continue;
+    long long kq = keep_index(a, si, q);
+    if (!GUARD_OK(a.guard, kq >= a.kstart[si] && kq < a.kstart[si + 1], 64, kq)) continue;
+    uf_unite(a.uf, uf_find(a.uf, (int)kk), uf_find(a.uf, (int)kq), a.err);
+    ++linked;
+  }
+}
+
+// (2) one warp per clustered subspace: a dense point of the dominant component
+__global__ void k_uf_sample(ClusterArgs a, int nclustered, int* __restrict__ sample) {
+  const int cs = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (cs >= nclustered) return;
+  const unsigned lane = lane_id();
+  const int si = a.clustered_list[cs];
+  const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+  const long long s0 = a.kstart[si], len = a.kstart[si + 1] - s0;
+  long long pick = -1;
+  if (len > 0) {
+    long long idx = s0 + ((2 * (long long)lane + 1) * len) / 64;
+    for (int t = 0; t < 16 && idx < s0 + len; ++t, ++idx)
+      if (bit_of(dn, a.keep_ids[idx])) {
+        pick = idx;
+        break;
+      }
+  }
+  const int root = pick >= 0 ? uf_find(a.uf, (int)pick) : -1 - (int)lane;  // no point: a unique non-root
+  const unsigned peers = __match_any_sync(0xffffffffu, root);
+  int votes = pick >= 0 ? __popc(peers) : 0;
+  int best = votes, who = (int)lane;
+  for (int o = 16; o > 0; o >>= 1) {
+    int bv = __shfl_xor_sync(0xffffffffu, best, o), bw = __shfl_xor_sync(0xffffffffu, who, o);
+    if (bv > best || (bv == best && bw < who)) {
+      best = bv;
+      who = bw;
+    }
+  }
+  long long win = __shfl_sync(0xffffffffu, pick, who);
+  if (lane == 0) sample[cs] = best > 0 ? (int)win : -1;
+}
+
+// (3) one warp per kept point outside the dominant component: all its dense
+// neighbours; the point's own root is found once per 32 neighbours
+__global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const int* __restrict__ cslot_of,
+                                                  const int* __restrict__ sample) {
   const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (kk >= a.nkeep) return;
   const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
@@ -98,17 +161,21 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a) {
   const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
   const int p = a.keep_ids[kk];
   if (!bit_of(dn, p)) return;
+  const unsigned lane = lane_id();
+  const int smp = sample[cslot_of[si]];
+  int skip = 0;
+  if (lane == 0 && smp >= 0) skip = uf_find(a.uf, (int)kk) == uf_find(a.uf, smp);
+  if (__shfl_sync(0xffffffffu, skip, 0)) return;
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
-  const unsigned lane = lane_id();
   for (int j0 = 0; j0 < len; j0 += 32) {
     const int j = j0 + (int)lane;
     int kq = -1;
     if (j < len) {
       int q = a.lids[b + j];
-      if (bit_of(dn, q)) {
+      if (GUARD_OK(a.guard, q >= 0 && q < a.n, 61, q) && bit_of(dn, q)) {
         long long k2 = keep_index(a, si, q);
-        if (k2 < kk) kq = (int)k2;  // each edge once, from its larger end
+        if (GUARD_OK(a.guard, k2 >= a.kstart[si] && k2 < a.kstart[si + 1], 62, k2)) kq = (int)k2;
       }
     }
     if (!__any_sync(0xffffffffu, kq >= 0)) continue;
@@ -181,7 +248,7 @@ __global__ void __launch_bounds__(256) k_borders(ClusterArgs a, const int* __res
   int* sl = slots + (long long)cslot_of[si] * a.n * 2;
   for (int j = lane_id(); j < len; j += 32) {
     int q = a.lids[b + j];
-    if (bit_of(dn, q)) continue;
+    if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 65, q) || bit_of(dn, q)) continue;
     int* s2 = sl + 2LL * q;
     int v0 = ((volatile int*)s2)[0];
     if (v0 == c) continue;
@@ -255,7 +322,11 @@ __global__ void __launch_bounds__(256) k_region_order(ClusterArgs a, const int* 
     const int m = C.npts;
     for (int j = threadIdx.x; j < m; j += blockDim.x) {
       int p = P[j];
-      if (bit_of(dn, p)) atomicMin(&firstpos[comp[keep_index(a, si, p)]], j);
+      if (bit_of(dn, p)) {
+        long long kp = keep_index(a, si, p);
+        if (GUARD_OK(a.guard, kp >= a.kstart[si] && kp < a.kstart[si + 1] && comp[kp] >= 0, 66, kp))
+          atomicMin(&firstpos[comp[kp]], j);
+      }
     }
     __syncthreads();
     int base = 0;
@@ -265,8 +336,11 @@ __global__ void __launch_bounds__(256) k_region_order(ClusterArgs a, const int* 
       if (j < m) {
         int p = P[j];
         if (bit_of(dn, p)) {
-          c = comp[keep_index(a, si, p)];
-          f = firstpos[c] == j;
+          long long kp = keep_index(a, si, p);
+          if (kp >= a.kstart[si] && kp < a.kstart[si + 1] && comp[kp] >= 0) {
+            c = comp[kp];
+            f = firstpos[c] == j;
+          }
         }
       }
       int tot;
@@ -277,7 +351,10 @@ __global__ void __launch_bounds__(256) k_region_order(ClusterArgs a, const int* 
     __syncthreads();
     for (int j = threadIdx.x; j < m; j += blockDim.x) {
       int p = P[j];
-      if (bit_of(dn, p)) firstpos[comp[keep_index(a, si, p)]] = INT_MAX;
+      if (bit_of(dn, p)) {
+        long long kp = keep_index(a, si, p);
+        if (kp >= a.kstart[si] && kp < a.kstart[si + 1] && comp[kp] >= 0) firstpos[comp[kp]] = INT_MAX;
+      }
     }
     if (threadIdx.x == 0) order_cnt[call] = base;
     __syncthreads();
@@ -304,8 +381,11 @@ void launch_pack_order(const CallDesc* ncalls, int ncall, const int* order, cons
 void launch_uf_init(int* par, long long n, cudaStream_t s) {
   if (n > 0) k_uf_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(par, n);
 }
-void launch_uf_union(const ClusterArgs& a, cudaStream_t s) {
-  if (a.nkeep > 0) k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a);
+void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, cudaStream_t s) {
+  if (a.nkeep <= 0) return;
+  k_uf_link2<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a);
+  if (nclustered > 0) k_uf_sample<<<(unsigned)((nclustered * 32LL + 255) / 256), 256, 0, s>>>(a, nclustered, sample);
+  k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a, cslot_of, sample);
 }
 void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s) {
   if (a.nkeep > 0) k_uf_flatten<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, is_root, root_of);

@@ -62,6 +62,10 @@ struct DensityArgs {
   float* lacc;
   unsigned long long* cand_counter;  // candidate tests (candidate x child subspace)
   unsigned long long* list_counter;  // list entries read
+  long long prev_total;  // entries in the previous level's lists
+  long long total;       // entries in this level's lists (write passes)
+  long long prev_nkeep;  // kept points of the previous level
+  Guard guard;
 };
 
 __device__ __forceinline__ int find_sub(const SubDesc* subs, int nsubs, long long item) {
@@ -107,7 +111,9 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
   const long long item = S.item_off + i;
   const bool level1 = S.parent < 0;
   const int D = S.dim;
+  if (!GUARD_OK(a.guard, level1 || S.query_off + i < a.prev_nkeep, 21, S.query_off + i)) return;
   const int p = level1 ? (int)i : a.prev_keep[S.query_off + i];
+  if (!GUARD_OK(a.guard, p >= 0 && p < a.n, 22, p)) return;
   const float xp = a.X[(size_t)p * a.d + D];
   const int fp = a.fc[(size_t)p * a.d + D];
   const int* ids;
@@ -122,6 +128,7 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     ids = a.prev_lids + b;
     accs = a.prev_lacc + b;
     len = a.prev_lcnt[S.query_off + i];
+    if (!GUARD_OK(a.guard, b >= 0 && len >= 0 && b + len <= a.prev_total, 23, b + len)) return;
   }
   int count = 0;
   const long long wbase = kWrite ? a.loff[item] : 0;
@@ -129,6 +136,7 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     long long j = j0 + lane;
     bool ok = j < len;
     int q = ok ? ids[j] : -1;
+    if (ok && !GUARD_OK(a.guard, q >= 0 && q < a.n, 24, q)) ok = false;
     ok = ok && q != p;
     if (ok && !level1) {
       int fq = a.fc[(size_t)q * a.d + D];
@@ -143,8 +151,10 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     unsigned m = __ballot_sync(0xffffffffu, ok);
     if (kWrite && ok) {
       long long o = wbase + count + __popc(m & lanemask_lt());
-      a.lids[o] = q;
-      a.lacc[o] = acc2;
+      if (GUARD_OK(a.guard, o >= 0 && o < a.total, 25, o)) {
+        a.lids[o] = q;
+        a.lacc[o] = acc2;
+      }
     }
     count += __popc(m);
   }
@@ -178,11 +188,14 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
   if (i < 0 || i >= g.nquery) return;  // unreachable when the offsets are consistent
   const int nc = g.nchild;
   const SubDesc& S0 = a.subs[g.sub_base];
+  if (!GUARD_OK(a.guard, S0.query_off + i < a.prev_nkeep && nc <= 64, 31, S0.query_off + i)) return;
   const int p = a.prev_keep[S0.query_off + i];
+  if (!GUARD_OK(a.guard, p >= 0 && p < a.n, 32, p)) return;
   const long long pb = a.prev_loff[S0.query_off + i];
   const int* ids = a.prev_lids + pb;
   const float* accs = a.prev_lacc + pb;
   const long long len = a.prev_lcnt[S0.query_off + i];
+  if (!GUARD_OK(a.guard, pb >= 0 && len >= 0 && pb + len <= a.prev_total, 33, pb + len)) return;
   const float* xrow_p = a.X + (size_t)p * a.d;
   const uint8_t* frow_p = a.fc + (size_t)p * a.d;
   int run0 = 0, run1 = 0;  // lane c: children c and c + 32
@@ -193,8 +206,12 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
   }
   for (long long j0 = 0; j0 < len; j0 += 32) {
     const long long j = j0 + lane;
-    const bool in = j < len;
-    const int q = in ? ids[j] : p;
+    bool in = j < len;
+    int q = in ? ids[j] : p;
+    if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
+      in = false;
+      q = p;
+    }
     const float acc = in ? accs[j] : 0.f;
     const float* xrow_q = a.X + (size_t)q * a.d;
     const uint8_t* frow_q = a.fc + (size_t)q * a.d;
@@ -215,8 +232,10 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
         long long base = __shfl_sync(0xffffffffu, c < 32 ? ob0 + run0 : ob1 + run1, owner);
         if (ok) {
           long long o = base + __popc(m & lanemask_lt());
-          a.lids[o] = q;
-          a.lacc[o] = acc2;
+          if (GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) {
+            a.lids[o] = q;
+            a.lacc[o] = acc2;
+          }
         }
       }
       if ((int)lane == (c & 31)) {
@@ -249,6 +268,7 @@ __global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
   if (a.rect) {
     v = (float)c;
   } else {
+    if (!GUARD_OK(a.guard, c >= 0 && a.loff[item] + c <= a.total, 41, a.loff[item] + c)) return;
     const float* acc = a.lacc + a.loff[item];
     float sum = 0.f;
     for (int j = 0; j < c; ++j) {
@@ -384,6 +404,10 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.lacc = L.lacc;
   a.cand_counter = L.cand_counter;
   a.list_counter = L.list_counter;
+  a.prev_total = L.prev_total;
+  a.total = L.total;
+  a.prev_nkeep = L.prev_nkeep;
+  a.guard = L.guard;
   return a;
 }
 

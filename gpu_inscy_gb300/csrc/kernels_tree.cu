@@ -67,6 +67,9 @@ struct TreeArgs {
   unsigned long long* out_ghost_top;
   long long out_ghost_cap;
   int* err;
+  long long pts_in_total;
+  long long ghosts_in_total;
+  Guard guard;
 };
 
 template <class Pred>
@@ -217,6 +220,10 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   const int np = C.npts;
   const int2* Gh = a.ghosts_in + C.ghost_off;
   const int ng = C.nghost;
+  if (!GUARD_OK(a.guard, C.pts_off >= 0 && C.pts_off + np <= a.pts_in_total, 51, C.pts_off + np)) return;
+  if (!GUARD_OK(a.guard, ng == 0 || (C.ghost_off >= 0 && C.ghost_off + ng <= a.ghosts_in_total), 52,
+                C.ghost_off + ng))
+    return;
   const uint64_t smask = C.rmask | (1ull << D);
   const SubDesc& S = a.subs[C.child_sub + (D - C.f)];
   const unsigned* wd = a.bitmaps + S.bitmap_off;
@@ -233,6 +240,15 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
   int* GB = GA + ng;
   RegionRec* rec = a.recs + (long long)w * a.cells;
 
+  // 0. the call's points and chains must be valid ids (checked once)
+  if (threadIdx.x == 0) s.gcount = 0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < np; j += blockDim.x)
+    if (!GUARD_OK(a.guard, P[j] >= 0 && P[j] < a.n, 53, P[j])) s.gcount = 1;
+  for (int j = threadIdx.x; j < ng; j += blockDim.x)
+    if (!GUARD_OK(a.guard, Gh[j].x >= 0 && Gh[j].x < a.n && Gh[j].y >= 0 && Gh[j].y < d, 54, Gh[j].x)) s.gcount = 1;
+  __syncthreads();
+  if (s.gcount) return;
   // 1. cell counts and s-connection flags on D
   for (int i = threadIdx.x; i < a.cells; i += blockDim.x) {
     s.cnt[i] = 0;
@@ -525,6 +541,9 @@ void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
   a.out_ghost_top = L.out_ghost_top;
   a.out_ghost_cap = L.out_ghost_cap;
   a.err = L.err;
+  a.pts_in_total = L.pts_in_total;
+  a.ghosts_in_total = L.ghosts_in_total;
+  a.guard = L.guard;
   k_tree_level<<<L.nwork, kTreeThreads, 0, s>>>(a);
 }
 
