@@ -84,6 +84,7 @@ __device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) 
     if (f) out[base + inc - 1] = x;
     base += tot;
   }
+  __syncthreads();  // the compacted entries are read by other threads next
   return base;
 }
 
