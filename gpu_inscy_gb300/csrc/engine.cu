@@ -706,6 +706,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       stats_.candidates += (long long)nc[0];
       stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] + (level == 1 ? 0.0 : 5.0 * (double)nc[0]);
     }
+    check_guard("density count");  // the counts size every later buffer
     DL.cand_counter = nullptr;
     DL.list_counter = nullptr;
 
