@@ -233,29 +233,30 @@ struct Entry {
 };
 
 // The clustering vector of one dim loop (InscyNodeCpu.cu:175): n labels,
-// -1 by default.  A generation stamp per point makes clearing it O(1).
+// -1 by default.  Each point holds (generation << 32 | label) in one word; a
+// label only counts when its generation is the current one, which makes
+// clearing the vector O(1).
 struct LoopVec {
-  std::vector<int> val;
-  std::vector<unsigned> gen;
-  unsigned cur = 1;
+  std::vector<uint64_t> gv;
+  uint64_t cur = 1ull << 32;
   void init(long long n) {
-    if ((long long)val.size() != n) {
-      val.assign(n, -1);
-      gen.assign(n, 0);
-      cur = 1;
+    if ((long long)gv.size() != n) {
+      gv.assign(n, 0);
+      cur = 1ull << 32;
     }
   }
   void clear() {
-    if (++cur == 0) {  // wrapped: reset the stamps
-      std::fill(gen.begin(), gen.end(), 0u);
-      cur = 1;
+    cur += 1ull << 32;
+    if (cur == 0) {  // wrapped: reset the stamps
+      std::fill(gv.begin(), gv.end(), 0ull);
+      cur = 1ull << 32;
     }
   }
-  int get(int p) const { return gen[p] == cur ? val[p] : -1; }
-  void set(int p, int v) {
-    gen[p] = cur;
-    val[p] = v;
+  int get(int p) const {
+    const uint64_t w = gv[p];
+    return (w & 0xffffffff00000000ull) == cur ? (int)(uint32_t)w : -1;
   }
+  void set(int p, int v) { gv[p] = cur | (uint32_t)v; }
 };
 
 // The clusters numbered in one dim loop (the reference's shared clustering
@@ -356,6 +357,7 @@ class Engine {
   std::vector<std::vector<int>> by_dim_;      // entries whose subspace holds each dim
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<LoopVec> vbuf_;                  // one clustering vector per recursion depth
+  std::vector<char> alive_;                    // join: clusters of the loop still alive
   double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
   long long* rc_ = nullptr;  // stats_.replay_counters
   inscy_stats stats_;
@@ -1092,7 +1094,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
 
   // ---------------------------------------------------------------- commit
   auto t_rep0 = std::chrono::steady_clock::now();
-  vbuf_.assign(d + 2, LoopVec());
+  if ((int)vbuf_.size() != d + 2) vbuf_.assign(d + 2, LoopVec());
   tbits_.assign(((size_t)n + 63) / 64, 0);
   t_prune_ = t_cluster_ = t_join_ = 0;
   rc_ = stats_.replay_counters;
@@ -1270,7 +1272,8 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   const int nl = st.nlabels;
   if (nl == 0) return;
   rc_[0]++;
-  std::vector<char> alive(nl + 1, 0);
+  std::vector<char>& alive = alive_;
+  alive.assign(nl + 1, 0);
   int minsz = INT32_MAX;
   for (int l = 1; l <= nl; ++l)
     if (st.size[l] >= hp_.min_size) {

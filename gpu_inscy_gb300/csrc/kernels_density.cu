@@ -272,12 +272,10 @@ __global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
     if (!GUARD_OK(a.guard, c >= 0 && lo >= 0 && lo + c <= a.total, 41, lo + c)) return;
     const float* acc = a.lacc + lo;
     float sum = 0.f;
-    // the double-precision step measured faster here than its integer form
-    // (phi_step_exact, kept for the device self-test)
 #pragma unroll 4
     for (int j = 0; j < c; ++j) {
       const float dd = __fdiv_rn(__fsqrt_rn(acc[j]), a.eps);
-      sum = phi_step_double(sum, __fmul_rn(dd, dd));
+      sum = phi_step_exact(sum, __fmul_rn(dd, dd));  // integer pipe, no FP64
     }
     v = sum;
   }

@@ -1,16 +1,21 @@
 // The reference's phi step, sum = float(double(sum) + (1.0 - double(sq)))
-// (ClusteringCpu.cu:118-120), computed exactly with integer arithmetic.
+// (ClusteringCpu.cu:118-120), computed exactly with 64-bit integer arithmetic.
 //
 // GB300's FP64 rate is a small fraction of its FP32/INT32 rate, and this step
-// runs once per (neighbour, subspace, point).  Both operands live on a common
-// fixed-point grid: sum is 0 or >= 2^-24 (it only ever grows by terms that
-// are 0 or >= 2^-24), so its bits sit at or above 2^-47; the term 1 - sq is
-// kept exactly on the 2^-53 grid (when sq < 2^-30 it is first rounded to that
-// grid exactly as the double subtraction rounds it).  The exact sum in units
-// of 2^-53 fits in 128 bits; rounding it to 53 significant bits (the double
-// addition) and then to 24 bits (the conversion to float), both to nearest
-// even, reproduces the reference's two roundings.  Sums of 2^60 and above
-// (never reached: a sum of at most n terms <= 1) take the double path.
+// runs once per (neighbour, subspace, point).  In units of 2^-53:
+//   * k = sq * 2^53, rounded to an integer as the double subtraction 1 - sq
+//     rounds (exact for sq >= 2^-30; ties to even below);
+//   * T = 2^53 - k is then exactly the double 1 - sq;
+//   * sum is 0 or >= 2^-24 (it only grows by terms that are 0 or >= 2^-24),
+//     so for sum < 2^10 it is an integer ms << (es + 30) below 2^63 and
+//     U = sum + T fits 64 bits exactly.  For larger sums the work moves to
+//     units of 2^(es - 62): the bits of T dropped by that shift become a
+//     sticky bit, which is exact for both roundings since they happen at
+//     least ten bits higher.
+// Rounding U to 53 significant bits (the double addition) and then to 24 (the
+// conversion to float), both to nearest even, reproduces the reference's two
+// roundings.  Inputs outside the domain (negative or subnormal sum, sq
+// outside [0, 1]) take the double expression.
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -23,24 +28,12 @@
 
 namespace inscy {
 
-typedef unsigned __int128 u128;
-
-PHI_HD int msb128(u128 v) {  // index of the highest set bit, v > 0
-  uint64_t hi = (uint64_t)(v >> 64), lo = (uint64_t)v;
+PHI_HD int msb64(uint64_t v) {  // index of the highest set bit, v > 0
 #ifdef __CUDA_ARCH__
-  return hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+  return 63 - __clzll((long long)v);
 #else
-  return hi ? 127 - __builtin_clzll(hi) : 63 - __builtin_clzll(lo);
+  return 63 - __builtin_clzll(v);
 #endif
-}
-
-// round v to a multiple of 2^r (r >= 1), ties to even
-PHI_HD u128 round_even(u128 v, int r) {
-  u128 q = v >> r;
-  u128 rem = v - (q << r);
-  u128 half = (u128)1 << (r - 1);
-  if (rem > half || (rem == half && (q & 1))) ++q;
-  return q << r;
 }
 
 PHI_HD uint32_t f2u(float f) {
@@ -62,57 +55,61 @@ PHI_HD float u2f(uint32_t u) {
 #endif
 }
 
-// double-precision reference of the step (used outside the exact range)
+// v rounded to a multiple of 2^r (r >= 1), ties to even; returns v >> r rounded
+PHI_HD uint64_t round_shift(uint64_t v, int r) {
+  const uint64_t q = v >> r, rem = v & ((1ull << r) - 1), half = 1ull << (r - 1);
+  return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+}
+
 PHI_HD float phi_step_double(float sum, float sq) {
   return (float)((double)sum + (1.0 - (double)sq));
 }
 
-// sum >= 0 (0 or >= 2^-24), sq in [0, 1]
 PHI_HD float phi_step_exact(float sum, float sq) {
   const uint32_t sb = f2u(sum), qb = f2u(sq);
-  const int es = (int)(sb >> 23) - 127;
-  if (sb != 0 && (es < -24 || es > 60)) return phi_step_double(sum, sq);
-  // T = (1 - sq) in units of 2^-53, rounded as the double subtraction does
-  uint64_t k;  // sq in units of 2^-53
-  if (qb == 0) {
-    k = 0;
-  } else {
-    const int eq = (int)(qb >> 23) - 127;  // sq <= 1: eq <= 0
-    const uint64_t mq = (qb & 0x7fffffu) | (((qb >> 23) != 0) ? 0x800000u : 0u);
-    const int sh = eq + 30;  // sq = mq * 2^(eq - 23) = mq * 2^(sh) * 2^-53
-    if ((qb >> 23) == 0) {
-      k = 0;  // subnormal sq < 2^-126: 1 - sq rounds to 1
-    } else if (sh >= 0) {
+  const uint32_t bs = sb >> 23, bq = qb >> 23;
+  if ((sb != 0 && (bs < 127 - 24 || bs > 254)) || qb > 0x3f800000u) return phi_step_double(sum, sq);
+  // k = sq in units of 2^-53, rounded as the double subtraction 1 - sq rounds
+  // (a subnormal sq leaves 1 - sq = 1: k = 0)
+  uint64_t k = 0;
+  if (bq != 0) {
+    const uint64_t mq = (qb & 0x7fffffu) | 0x800000u;
+    const int sh = (int)bq - 127 + 30;  // sq = mq * 2^sh units
+    if (sh >= 0)
       k = mq << sh;
-    } else if (sh < -40) {
-      k = 0;  // below half a unit of 2^-53
-    } else {
-      // round mq * 2^sh to an integer, ties to even (the result 2^53 - k then
-      // has an even last bit, as the double subtraction's tie rule requires)
-      const int r = -sh;
-      uint64_t q = mq >> r, rem = mq & ((1ull << r) - 1), half = 1ull << (r - 1);
-      if (rem > half || (rem == half && (q & 1))) ++q;
-      k = q;
-    }
+    else if (sh >= -24)
+      k = round_shift(mq, -sh);  // below that, mq * 2^sh < 1/2 rounds to 0
   }
   const uint64_t T = (1ull << 53) - k;
-  u128 V = (u128)T;
-  if (sb != 0) {
+  uint64_t U;
+  int g = 0;  // U is in units of 2^(g - 53)
+  if (sb == 0) {
+    U = T;
+  } else {
     const uint64_t ms = (sb & 0x7fffffu) | 0x800000u;
-    V += (u128)ms << (es + 30);  // sum = ms * 2^(es - 23) = ms << (es + 30) units
+    const int es = (int)bs - 127;
+    if (es <= 9) {
+      U = (ms << (es + 30)) + T;
+    } else {
+      g = es - 9;
+      const uint64_t Tg = g >= 64 ? (uint64_t)(T != 0) : ((T >> g) | (uint64_t)((T & ((1ull << g) - 1)) != 0));
+      U = (ms << 39) + Tg;
+    }
   }
-  if (V == 0) return 0.f;
-  // the double addition: 53 significant bits
-  int p = msb128(V);
-  if (p > 52) V = round_even(V, p - 52);
-  // the conversion to float: 24 significant bits
-  p = msb128(V);
-  if (p > 23) V = round_even(V, p - 23);
-  p = msb128(V);
-  // value = V * 2^-53 with V = m * 2^(p - 23), m in [2^23, 2^24)
-  const uint32_t m = (uint32_t)(V >> (p - 23));
-  const int e = p - 53;
-  return u2f(((uint32_t)(e + 127) << 23) | (m & 0x7fffffu));
+  if (U == 0) return 0.f;
+  // U >= 2^29 here (sum >= 2^-24 or 1 - sq >= 2^-24): both rounding shifts are >= 6
+  int p = msb64(U);
+  if (p > 52) {  // the double addition: 53 significant bits
+    U = round_shift(U, p - 52) << (p - 52);
+    p = msb64(U);
+  }
+  uint64_t q = round_shift(U, p - 23);  // the conversion to float: 24 significant bits
+  int e = p - 53 + g;                   // value = (q / 2^23) * 2^e
+  if (q >> 24) {                        // rounded up to 2^24
+    q >>= 1;
+    ++e;
+  }
+  return u2f(((uint32_t)(e + 127) << 23) | ((uint32_t)q & 0x7fffffu));
 }
 
 }  // namespace inscy
