@@ -31,6 +31,11 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 
 #include "../../include/inscy_gb300.h"
 #include "inscy_common.cuh"
@@ -267,6 +272,105 @@ struct LoopState {
   int nlabels = 0;
 };
 
+// Host threads for the data-parallel loops of the commit.  run(tasks, fn)
+// calls fn(i) for every i in [0, tasks) on the workers and the calling
+// thread and returns when all are done.
+class HostPool {
+ public:
+  explicit HostPool(int workers) {
+    for (int i = 0; i < workers; ++i) th_.emplace_back([this] { loop(); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  int workers() const { return (int)th_.size(); }
+  void run(int tasks, const std::function<void(int)>& fn) {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      fn_ = &fn;
+      tasks_ = tasks;
+      next_.store(0);
+      pending_ = (int)th_.size();
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(m_);
+    done_.wait(lk, [&] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  void work() {
+    for (;;) {
+      const int i = next_.fetch_add(1);
+      if (i >= tasks_) break;
+      (*fn_)(i);
+    }
+  }
+  void loop() {
+    long long seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+      }
+      work();
+      std::lock_guard<std::mutex> g(m_);
+      if (--pending_ == 0) done_.notify_all();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* fn_ = nullptr;
+  std::atomic<int> next_{0};
+  int tasks_ = 0, pending_ = 0;
+  long long gen_ = 0;
+  bool stop_ = false;
+};
+
+// Points [k0, k1) of a superset cluster's member list (the points still
+// labelled l in that entry count) for join's redundancy test.
+struct Walk {
+  const int* mem;
+  long long k0, k1;
+  const int* lab;
+  int l;
+  float hsz;
+};
+
+// Drop every live cluster c of the loop with a point in w and
+// size(c) * r < |w's cluster| (util.cu:680-705); true if one was dropped.
+static bool walk_test(const Walk& w, const LoopVec& V, const int* size, float r, char* alive) {
+  bool hit = false;
+  const uint64_t* gv = V.gv.data();
+  const uint64_t cur = V.cur;
+  for (long long k = w.k0; k < w.k1; ++k) {
+    const int q = w.mem[k];
+    if (w.lab[q] != w.l) continue;
+    const uint64_t x = gv[q];
+    if ((x & 0xffffffff00000000ull) != cur) continue;
+    const int c = (int)(uint32_t)x;
+    if (c > 0 && __atomic_load_n(&alive[c], __ATOMIC_RELAXED) && (float)size[c] * r < w.hsz) {
+      __atomic_store_n(&alive[c], (char)0, __ATOMIC_RELAXED);
+      hit = true;
+    }
+  }
+  return hit;
+}
+
+// joins whose redundancy test covers fewer points run it on one thread
+constexpr long long kParallelWalk = 32768;
+
 struct HostParams {
   float eps, F, r;
   int num_obj, min_size, cells, rect;
@@ -280,6 +384,10 @@ class Engine {
   Engine() {
     CK(cudaGetDevice(&device_));
     pool_.reset(new Pool(device_));
+    {
+      const int hw = (int)std::thread::hardware_concurrency();
+      hpool_.reset(new HostPool(std::max(0, std::min(7, hw / 2 - 1))));
+    }
     CK(cudaEventCreate(&ev0_));
     CK(cudaEventCreate(&ev1_));
   }
@@ -338,6 +446,7 @@ class Engine {
   const std::vector<int>& superset_candidates(uint64_t smask);
   void cluster_into(const HCall& c, LoopVec& V, LoopState& st);
   void join(LoopVec& V, LoopState& st, uint64_t smask);
+  void split_pieces(long long work);
 
   int device_ = 0;
   std::unique_ptr<Pool> pool_;
@@ -354,10 +463,13 @@ class Engine {
   std::vector<std::unique_ptr<Entry>> ents_;  // result map entries, in insertion order
   std::vector<uint64_t> emask_;               // their subspaces
   std::map<uint64_t, int> eidx_;              // subspace -> entry
-  std::vector<std::vector<int>> by_dim_;      // entries whose subspace holds each dim
+  std::vector<std::vector<uint64_t>> dim_bits_;  // per dim: bitset of the entries whose subspace holds it
+  std::vector<int> sup_;                         // superset_candidates' result
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<LoopVec> vbuf_;                  // one clustering vector per recursion depth
   std::vector<char> alive_;                    // join: clusters of the loop still alive
+  std::vector<Walk> walk_, pieces_, split_;   // point ranges of the commit's loops
+  std::unique_ptr<HostPool> hpool_;
   double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
   long long* rc_ = nullptr;  // stats_.replay_counters
   inscy_stats stats_;
@@ -377,7 +489,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   ents_.clear();
   emask_.clear();
   eidx_.clear();
-  by_dim_.assign(d, std::vector<int>());
+  dim_bits_.assign(d, std::vector<uint64_t>());
   out_dims.clear();
   out_labels.clear();
   if (n == 0) {
@@ -1160,18 +1272,20 @@ void Engine::replay(int ci) {
 // is decided; per entry the smallest touched cluster is found either by
 // scanning the region's points or, for large regions, by walking the entry's
 // clusters smallest-first against a bitmap of the region.
-// entries that may contain subspace `smask`: those holding its rarest dim
+// the entries whose subspace contains `smask`, in insertion order: the AND of
+// the per-dim entry bitsets over the dims of smask
 const std::vector<int>& Engine::superset_candidates(uint64_t smask) {
-  int best = -1;
-  size_t bs = SIZE_MAX;
-  for (uint64_t m = smask; m; m &= m - 1) {
-    int k = __builtin_ctzll(m);
-    if (by_dim_[k].size() < bs) {
-      bs = by_dim_[k].size();
-      best = k;
+  sup_.clear();
+  const size_t nw = (ents_.size() + 63) / 64;
+  for (size_t w = 0; w < nw; ++w) {
+    uint64_t x = ~0ull;
+    for (uint64_t m = smask; m && x; m &= m - 1) x &= dim_bits_[__builtin_ctzll(m)][w];
+    while (x) {
+      sup_.push_back((int)(w * 64 + __builtin_ctzll(x)));
+      x &= x - 1;
     }
   }
-  return by_dim_[best];
+  return sup_;
 }
 
 static void refresh_order(Entry& E) {
@@ -1189,12 +1303,10 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
   rc_[6]++;
   const double thr = (double)((float)m * hp_.r);
   const bool use_bits = (long long)m * 8 > n_;
-  if (use_bits)
-    for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] |= 1ull << (pts[j] & 63);
+  bool bits_set = false;  // the region's bitmap, built when first needed
   int max_min = 0;
   bool result = true;
   for (int i : superset_candidates(smask)) {
-    if ((emask_[i] & smask) != smask) continue;
     Entry& E = *ents_[i];
     int mn = -1;
     if (!use_bits) {
@@ -1207,6 +1319,10 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
         }
       }
     } else {
+      if (!bits_set) {
+        for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] |= 1ull << (pts[j] & 63);
+        bits_set = true;
+      }
       refresh_order(E);
       for (int l : E.by_size) {
         bool hit = false;
@@ -1234,8 +1350,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
       }
     }
   }
-  if (use_bits)
-    for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] = 0;
+  if (bits_set) std::fill(tbits_.begin(), tbits_.end(), 0ull);
   return max_min == 0 ? true : result;
 }
 
@@ -1245,22 +1360,65 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
 void Engine::cluster_into(const HCall& c, LoopVec& V, LoopState& st) {
   const HSub& hs = subs_[c.csub];
   const int* order = levels_[c.level].order.data() + c.order_off;
+  // labels in first-seed order.  Components are disjoint and their border
+  // points are not dense, so no write below changes another component's
+  // first member: all labels can be decided before the writes.
+  const int first = st.nlabels + 1;
+  long long work = 0;
   for (int t = 0; t < c.norder; ++t) {
     int comp = order[t];
     long long m0 = hs.moff[comp], m1 = hs.moff[comp + 1];
     if (m1 == m0) continue;
     if (V.get(hs.members[m0]) != -1) continue;  // already numbered in this dim loop
-    int label = ++st.nlabels;
+    ++st.nlabels;
     rc_[8]++;
     rc_[9] += hs.boff[comp + 1] - hs.boff[comp];
     st.ref.push_back(LabelRef{c.csub, comp});
     st.size.push_back((int)(m1 - m0));
-    for (long long k = m0; k < m1; ++k) V.set(hs.members[k], label);
-    for (long long k = hs.boff[comp]; k < hs.boff[comp + 1]; ++k) {
-      int q = hs.borders[k];
-      if (V.get(q) == -1) V.set(q, -2);
-    }
+    work += (m1 - m0) + (hs.boff[comp + 1] - hs.boff[comp]);
   }
+  // members get the label; non-dense neighbours that are still -1 become -2
+  // (the only other value they can hold here)
+  if (work < kParallelWalk || hpool_->workers() == 0) {
+    for (int label = first; label <= st.nlabels; ++label) {
+      const int comp = st.ref[label].comp;
+      for (long long k = hs.moff[comp]; k < hs.moff[comp + 1]; ++k) V.set(hs.members[k], label);
+      for (long long k = hs.boff[comp]; k < hs.boff[comp + 1]; ++k) {
+        const int q = hs.borders[k];
+        if (V.get(q) == -1) V.set(q, -2);
+      }
+    }
+    return;
+  }
+  pieces_.clear();
+  for (int label = first; label <= st.nlabels; ++label) {
+    const int comp = st.ref[label].comp;
+    pieces_.push_back(Walk{hs.members.data() + hs.moff[comp], 0, hs.moff[comp + 1] - hs.moff[comp], nullptr, label, 0.f});
+    pieces_.push_back(Walk{hs.borders.data() + hs.boff[comp], 0, hs.boff[comp + 1] - hs.boff[comp], nullptr, -2, 0.f});
+  }
+  uint64_t* gv = V.gv.data();
+  const uint64_t cur = V.cur;
+  split_pieces(work);
+  hpool_->run((int)split_.size(), [&](int i) {
+    const Walk& w = split_[i];
+    const uint64_t v = cur | (uint32_t)w.l;
+    if (w.l > 0) {
+      for (long long k = w.k0; k < w.k1; ++k) __atomic_store_n(&gv[w.mem[k]], v, __ATOMIC_RELAXED);
+    } else {
+      for (long long k = w.k0; k < w.k1; ++k) {
+        uint64_t* g = &gv[w.mem[k]];
+        if ((__atomic_load_n(g, __ATOMIC_RELAXED) & 0xffffffff00000000ull) != cur) __atomic_store_n(g, v, __ATOMIC_RELAXED);
+      }
+    }
+  });
+}
+
+// pieces_ cut into parts of about work / (4 * threads) entries (split_)
+void Engine::split_pieces(long long work) {
+  split_.clear();
+  const long long part = std::max(4096LL, work / (4LL * (hpool_->workers() + 1)));
+  for (const Walk& w : pieces_)
+    for (long long k = w.k0; k < w.k1; k += part) split_.push_back(Walk{w.mem, k, std::min(w.k1, k + part), w.lab, w.l, w.hsz});
 }
 
 // join (util.cu:655-743): drop clusters below min_size, drop clusters a
@@ -1281,22 +1439,17 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       minsz = std::min(minsz, st.size[l]);
     }
   if (minsz == INT32_MAX) return;
-  for (int i : superset_candidates(smask)) {
-    if ((emask_[i] & smask) != smask) continue;
-    Entry& H = *ents_[i];
-    rc_[4]++;
-    bool hit = false;
-    auto test = [&](int q, int hsz) {
-      rc_[5]++;
-      int c = V.get(q);
-      if (c > 0 && alive[c] && (float)st.size[c] * hp_.r < (float)hsz) {
-        alive[c] = 0;
-        hit = true;
-      }
-    };
-    if (hp_.r >= 0.f) {
-      // only clusters of H larger than (smallest cluster here) * r can drop
-      // anything; walk them largest first (float comparisons as the reference)
+  if (hp_.r >= 0.f) {
+    // Only clusters of a superset entry larger than (smallest cluster here) * r
+    // can drop anything (float comparisons as the reference).  Whether a
+    // cluster here is dropped does not depend on the order of the tests, so
+    // the points of all such clusters are tested together, split over the
+    // host pool when there are many.
+    walk_.clear();
+    long long total = 0;
+    for (int i : superset_candidates(smask)) {
+      Entry& H = *ents_[i];
+      rc_[4]++;
       if (!((float)minsz * hp_.r < (float)H.maxsz)) continue;
       refresh_order(H);
       for (int t = (int)H.by_size.size() - 1; t >= 0; --t) {
@@ -1305,28 +1458,69 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         if (!((float)minsz * hp_.r < (float)hsz)) break;
         const HSub& hs = subs_[H.src[l].csub];
         const int cp = H.src[l].comp;
-        for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
-          int q = hs.members[k];
-          if (H.lab[q] == l) test(q, hsz);
+        const long long m = hs.moff[cp + 1] - hs.moff[cp];
+        walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, m, H.lab.data(), l, (float)hsz});
+        total += m;
+      }
+    }
+    rc_[5] += total;
+    bool hit = false;
+    const int* ssz = st.size.data();
+    const float r = hp_.r;
+    if (total < kParallelWalk || hpool_->workers() == 0) {
+      // one thread: raise the size bar as clusters drop
+      for (const Walk& w : walk_) {
+        if (!((float)minsz * r < w.hsz)) continue;
+        if (walk_test(w, V, ssz, r, alive.data())) {
+          hit = true;
+          minsz = INT32_MAX;
+          for (int l = 1; l <= nl; ++l)
+            if (alive[l]) minsz = std::min(minsz, st.size[l]);
+          if (minsz == INT32_MAX) return;
         }
       }
     } else {
-      for (int l = 1; l <= nl; ++l) {
-        if (!alive[l]) continue;
-        const HSub& hs = subs_[st.ref[l].csub];
-        const int cp = st.ref[l].comp;
-        for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
-          int q = hs.members[k];
-          int h = H.lab[q];
-          if (h >= 0) test(q, H.size[h]);
-        }
-      }
+      pieces_.assign(walk_.begin(), walk_.end());
+      split_pieces(total);
+      std::atomic<bool> any{false};
+      hpool_->run((int)split_.size(), [&](int i) {
+        if (walk_test(split_[i], V, ssz, r, alive.data())) any.store(true, std::memory_order_relaxed);
+      });
+      hit = any.load();
     }
     if (hit) {
       minsz = INT32_MAX;
       for (int l = 1; l <= nl; ++l)
         if (alive[l]) minsz = std::min(minsz, st.size[l]);
       if (minsz == INT32_MAX) return;
+    }
+  } else {
+    for (int i : superset_candidates(smask)) {
+      Entry& H = *ents_[i];
+      rc_[4]++;
+      bool hit = false;
+      for (int l = 1; l <= nl; ++l) {
+        if (!alive[l]) continue;
+        const HSub& hs = subs_[st.ref[l].csub];
+        const int cp = st.ref[l].comp;
+        for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+          const int q = hs.members[k];
+          const int h = H.lab[q];
+          rc_[5]++;
+          if (h < 0) continue;
+          const int c = V.get(q);
+          if (c > 0 && alive[c] && (float)st.size[c] * hp_.r < (float)H.size[h]) {
+            alive[c] = 0;
+            hit = true;
+          }
+        }
+      }
+      if (hit) {
+        minsz = INT32_MAX;
+        for (int l = 1; l <= nl; ++l)
+          if (alive[l]) minsz = std::min(minsz, st.size[l]);
+        if (minsz == INT32_MAX) return;
+      }
     }
   }
   Entry* E;
@@ -1342,7 +1536,10 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     E = ne.get();
     rc_[1]++;
     eidx_[smask] = (int)ents_.size();
-    for (uint64_t m = smask; m; m &= m - 1) by_dim_[__builtin_ctzll(m)].push_back((int)ents_.size());
+    const size_t e = ents_.size();
+    for (auto& b : dim_bits_)
+      if (b.size() * 64 <= e) b.push_back(0);
+    for (uint64_t m = smask; m; m &= m - 1) dim_bits_[__builtin_ctzll(m)][e >> 6] |= 1ull << (e & 63);
     ents_.push_back(std::move(ne));
     emask_.push_back(smask);
     off = 0;
@@ -1352,28 +1549,66 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     E->size.resize(top + 1, 0);
     E->src.resize(top + 1, LabelRef{-1, -1});
   }
+  // label sizes and sources, then the point writes: members of the live
+  // clusters get their new label, border marks of every cluster overwrite
+  // (util.cu:726-739); a relabelled point leaves its old cluster
+  pieces_.clear();
+  long long work = 0;
   for (int l = 1; l <= nl; ++l) {
     const HSub& hs = subs_[st.ref[l].csub];
     const int cp = st.ref[l].comp;
     if (alive[l]) {
       const int nv = off + l;
-      for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
-        int p = hs.members[k];
-        int ov = E->lab[p];
-        if (ov >= 0) E->size[ov]--;
-        E->lab[p] = nv;
-      }
       E->size[nv] += st.size[l];
       E->src[nv] = st.ref[l];
       rc_[2] += st.size[l];
+      pieces_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, hs.moff[cp + 1] - hs.moff[cp], nullptr, nv, 0.f});
+      work += hs.moff[cp + 1] - hs.moff[cp];
     }
     rc_[3] += hs.boff[cp + 1] - hs.boff[cp];
-    for (long long k = hs.boff[cp]; k < hs.boff[cp + 1]; ++k) {
-      int q = hs.borders[k];
-      int ov = E->lab[q];
-      if (ov >= 0) E->size[ov]--;
-      E->lab[q] = -2;
+    pieces_.push_back(Walk{hs.borders.data() + hs.boff[cp], 0, hs.boff[cp + 1] - hs.boff[cp], nullptr, -2, 0.f});
+    work += hs.boff[cp + 1] - hs.boff[cp];
+  }
+  int* lab = E->lab.data();
+  int* esz = E->size.data();
+  if (work < kParallelWalk || hpool_->workers() == 0) {
+    for (const Walk& w : pieces_) {
+      if (w.l >= 0) {
+        for (long long k = w.k0; k < w.k1; ++k) {
+          const int p = w.mem[k];
+          const int ov = lab[p];
+          if (ov >= 0) esz[ov]--;
+          lab[p] = w.l;
+        }
+      } else {
+        for (long long k = w.k0; k < w.k1; ++k) {
+          const int q = w.mem[k];
+          const int ov = lab[q];
+          if (ov >= 0) esz[ov]--;
+          lab[q] = -2;
+        }
+      }
     }
+  } else {
+    // members of different clusters are disjoint and never border points;
+    // a border point may be listed by several clusters, hence the exchange
+    split_pieces(work);
+    hpool_->run((int)split_.size(), [&](int i) {
+      const Walk& w = split_[i];
+      if (w.l >= 0) {
+        for (long long k = w.k0; k < w.k1; ++k) {
+          const int p = w.mem[k];
+          const int ov = lab[p];
+          if (ov >= 0) __atomic_fetch_sub(&esz[ov], 1, __ATOMIC_RELAXED);
+          lab[p] = w.l;
+        }
+      } else {
+        for (long long k = w.k0; k < w.k1; ++k) {
+          const int ov = __atomic_exchange_n(&lab[w.mem[k]], -2, __ATOMIC_RELAXED);
+          if (ov >= 0) __atomic_fetch_sub(&esz[ov], 1, __ATOMIC_RELAXED);
+        }
+      }
+    });
   }
   // v_max over the whole vector: the largest label that still has points,
   // else the largest of -1/-2 present
