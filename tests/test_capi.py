@@ -80,8 +80,10 @@ def test_result_accessors_tolerate_null(engine):
     engine.inscy_result_free(None)
 
 
-def test_missing_library_fails_loudly(monkeypatch, tmp_path):
-    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
+def test_missing_library_fails_loudly(monkeypatch):
+    missing = os.path.join(os.path.dirname(_lib.LIB_PATH), "_build", "no_such_library.so")
+    assert not os.path.exists(missing)
+    monkeypatch.setattr(_lib, "LIB_PATH", missing)
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(ImportError):
         _lib.load()

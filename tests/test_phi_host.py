@@ -12,11 +12,13 @@ import subprocess
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(os.path.dirname(HERE), "gpu_inscy_gb300", "_build")
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
-def test_phi_step_exact_matches_double(tmp_path):
-    exe = str(tmp_path / "phi_host_check")
+def test_phi_step_exact_matches_double():
+    os.makedirs(BUILD, exist_ok=True)
+    exe = os.path.join(BUILD, "phi_host_check")
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(HERE, "phi_host_check.cpp"),
                     "-o", exe], check=True)
     out = subprocess.run([exe, "20000000"], check=True, capture_output=True, text=True).stdout.split()
