@@ -18,6 +18,7 @@
 //
 // One warp per (subspace, query point); candidates are consumed 32 at a time
 // with a ballot, and phi is accumulated over the accepted lanes in order.
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -254,41 +255,75 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
   }
 }
 
-// density of one (subspace, point) from its list, one thread each (the phi
-// sum is sequential; every lane works on its own point)
-__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
-  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.nitems) return;
+// density of every (subspace, point) from its list.  The phi sum of one item
+// is sequential, so each lane walks its own list; lists differ a lot in
+// length, so every warp owns kFlagsItems consecutive items as a queue: a lane
+// that finishes an item takes the next one, and all busy lanes advance
+// together for as many entries as the shortest remaining list allows.
+constexpr int kFlagsItems = 256;
+
+__device__ __forceinline__ void flags_finish(const DensityArgs& a, long long item, float v) {
   const int si = find_sub(a.subs, a.nsubs, item);
   const SubDesc& S = a.subs[si];
   const long long i = item - S.item_off;
   const int p = S.parent < 0 ? (int)i : a.prev_keep[S.query_off + i];
-  const int c = a.cnt[item];
-  float v;
-  if (a.rect) {
-    v = (float)c;
-  } else {
-    const long long lo = a.loff[item];
-    if (!GUARD_OK(a.guard, c >= 0 && lo >= 0 && lo + c <= a.total, 41, lo + c)) return;
-    const float* acc = a.lacc + lo;
-    float sum = 0.f;
-#pragma unroll 4
-    for (int j = 0; j < c; ++j) {
-      const float dd = __fdiv_rn(__fsqrt_rn(acc[j]), a.eps);
-      sum = phi_step_exact(sum, __fmul_rn(dd, dd));  // integer pipe, no FP64
-    }
-    v = sum;
-  }
   uint8_t f = 0;
   if (v >= a.thr_weak) f |= kFlagWeak;
   if (v >= a.thr_dense[S.nsub]) f |= kFlagDense;
   if (v >= a.thr_keep[S.nsub]) f |= kFlagKeep;
   a.flags[item] = f;
-  unsigned bit = 1u << (p & 31);
+  const unsigned bit = 1u << (p & 31);
   unsigned* bm = a.bitmaps + S.bitmap_off + (p >> 5);
   if (f & kFlagWeak) atomicOr(bm, bit);
   if (f & kFlagDense) atomicOr(bm + a.words, bit);
   if (f & kFlagKeep) atomicOr(bm + 2 * a.words, bit);
+}
+
+__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
+  const long long first = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kFlagsItems;
+  if (first >= a.nitems) return;  // whole warps
+  const long long last = first + kFlagsItems < a.nitems ? first + kFlagsItems : a.nitems;
+  const unsigned lane = lane_id();
+  long long next = first + 32;  // next item of the queue (the same in every lane)
+  long long item = first + lane;
+  const float* acc = nullptr;
+  int c = 0, j = 0;
+  float sum = 0.f;
+  bool live = false;  // this lane holds an item whose flags are still to be written
+  auto take = [&](long long it) {
+    item = it;
+    live = false;
+    if (it >= last) return;
+    c = a.cnt[it];
+    const long long lo = a.loff[it];
+    if (!GUARD_OK(a.guard, c >= 0 && lo >= 0 && lo + c <= a.total, 41, lo + c)) return;
+    acc = a.lacc + lo;
+    j = a.rect ? c : 0;  // rectangular density: the neighbour count, no sum
+    sum = 0.f;
+    live = true;
+  };
+  take(item);
+  for (;;) {
+    if (!__any_sync(0xffffffffu, live)) break;
+    // steps every busy lane can take: the shortest remaining list
+    int steps = live ? c - j : INT_MAX;
+    for (int o = 16; o > 0; o >>= 1) steps = min(steps, __shfl_xor_sync(0xffffffffu, steps, o));
+    if (live) {
+      for (int t = 0; t < steps; ++t) {
+        const float dd = __fdiv_rn(__fsqrt_rn(acc[j + t]), a.eps);
+        sum = phi_step_exact(sum, __fmul_rn(dd, dd));  // integer pipe, no FP64
+      }
+      j += steps;
+    }
+    const bool done = live && j >= c;
+    if (done) flags_finish(a, item, a.rect ? (float)c : sum);
+    const unsigned need = __ballot_sync(0xffffffffu, done || (!live && item < last));
+    if (need) {
+      const long long mine = next + __popc(need & lanemask_lt());
+      if ((need >> lane) & 1u) take(mine);
+      next += __popc(need);
+    }
+  }
 }
 
 // kept items: list lengths (0 for the others) for the offset scan
@@ -472,7 +507,8 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s) {
   if (L.nitems <= 0) return;
   DensityArgs a = make_args(L);
-  k_density_flags<<<(unsigned)((L.nitems + 255) / 256), 256, 0, s>>>(a);
+  const long long warps = (L.nitems + kFlagsItems - 1) / kFlagsItems;
+  k_density_flags<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(a);
 }
 
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
