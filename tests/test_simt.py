@@ -1,0 +1,83 @@
+"""The engine's CUDA sources executed on the host (tests/simt), checked
+against the reference outputs -- a CPU check of the kernels themselves.
+
+Every device allocation sits against a guard page, so an out-of-range or
+stale index in any kernel faults here; warp collectives must see all 32 lanes
+at the same call; and each case runs twice, with the warps of every block in
+ascending and in descending order, so a value one warp reads before another
+warp has written it without a barrier changes the result.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from golden_io import assert_same, family_cases, small_case
+from gpu_inscy_gb300 import synth
+import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "simt"))
+
+pytestmark = pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+
+
+@pytest.fixture(scope="module")
+def driver():
+    import build_simt
+    return build_simt.build()
+
+
+def simt_run(driver, X, p, reverse, tag):
+    out_dir = os.path.dirname(driver)
+    fx, fo = os.path.join(out_dir, tag + ".f32"), os.path.join(out_dir, tag + ".out")
+    X = np.ascontiguousarray(X, np.float32)
+    X.tofile(fx)
+    n, d = X.shape
+    args = [driver, fx, str(n), str(d), repr(float(p["neighborhood_size"])), repr(float(p["F"])), str(p["num_obj"]),
+            str(p["min_size"]), repr(float(p["r"])), str(p["number_of_cells"]), str(int(p.get("rectangular", 0))), fo]
+    env = dict(os.environ)
+    env.pop("SIMT_REVERSE", None)
+    if reverse:
+        env["SIMT_REVERSE"] = "1"
+    r = subprocess.run(args, capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    raw = np.fromfile(fo, np.int32)
+    k, pos, subs, labs = raw[0], 1, [], []
+    for _ in range(k):
+        m = raw[pos]
+        subs.append(raw[pos + 1:pos + 1 + m].tolist())
+        pos += 1 + m
+        labs.append(raw[pos:pos + n])
+        pos += n
+    return subs, (np.stack(labs) if labs else np.zeros((0, n), np.int32))
+
+
+@pytest.mark.parametrize("reverse", [False, True], ids=["warps-up", "warps-down"])
+@pytest.mark.parametrize("rect", [0, 1])
+def test_small_workload(driver, rect, reverse):
+    X, p, want = small_case(rect)
+    assert_same(simt_run(driver, X, p, reverse, "small%d" % rect), want, "small rect=%d" % rect)
+
+
+def test_family_cases(driver):
+    cases = [c for c in family_cases() if c[2]["entropy_order"] == 0][:12]
+    for i, X, p, want in cases:
+        assert_same(simt_run(driver, X, p, i % 2 == 1, "family%d" % i), want, "family %d" % i)
+
+
+@pytest.fixture(scope="module")
+def plain_case():
+    # the 25,000 x 15 workload's generator and parameters at a size the oracle finishes fast
+    X = synth.make_plain(3, n=1000)
+    p = dict(synth.PARAMS["plain"])
+    return X, p, orc.run(X, **p)
+
+
+@pytest.mark.parametrize("reverse", [False, True], ids=["warps-up", "warps-down"])
+def test_plain_workload_shape(driver, plain_case, reverse):
+    X, p, want = plain_case
+    assert_same(simt_run(driver, X, p, reverse, "plain"), want, "plain n=1000")
