@@ -191,7 +191,7 @@ class Pinned {
 struct HRegion {
   int dim;
   int passed;
-  int child;  // index into calls_ (passed only)
+  int child;  // index of the child call in its phase (passed only)
 };
 
 struct HCall {
@@ -199,10 +199,10 @@ struct HCall {
   int f = 0;
   int level = 0;
   int npts = 0;
-  long long pts_off = 0;  // into levels_[level].pts (its leaf order)
-  int norder = 0;         // components in first-seed order, at levels_[level].order[order_off ...]
+  long long pts_off = 0;  // into its level's pts (its leaf order)
+  int norder = 0;         // components in first-seed order, at its level's order[order_off ...]
   long long order_off = 0;
-  int csub = -1;          // clustered subspace (its own subspace) in subs_
+  int csub = -1;          // clustered subspace (its own subspace) in its phase's subs
   std::vector<HRegion> regions;  // ordered by (dim, cell run)
 };
 
@@ -218,11 +218,28 @@ struct HSub {  // components of one clustered subspace
   std::vector<int> borders;
 };
 
-// Where the points of a label come from: component `comp` of clustered
-// subspace `csub` (its member list is the GPU's).
+// Where the points of a label come from: component `comp` of a clustered
+// subspace (its member list is the GPU's).  A phase's subspaces do not move
+// once the phase is complete, which is before any label points to them.
 struct LabelRef {
-  int csub;
+  const HSub* hs;
   int comp;
+};
+
+// The calls whose first restricted dim lies in [d0, d1) (the root's
+// restrictions to those dims and everything below them).  INSCY's depth-first
+// commit handles them after the calls of every smaller first dim, and a
+// superset of their subspaces either holds a smaller dim (an earlier phase)
+// or starts in the same range (this phase), so a phase can be committed as
+// soon as its expansion is done, while the GPU expands the next one.  Phase k
+// covers the first dims [2^k - 1, 2^(k+1) - 1): the lattice below dim D shrinks
+// about geometrically with D, so the early phases hold comparable work and
+// the last one, whose commit is all that is left once the GPU is done, little.
+struct Phase {
+  int d0 = 0, d1 = 0;
+  std::vector<HCall> calls;    // level >= 1
+  std::vector<HLevel> levels;  // [level] for level >= 2 (level 1: the shared level1_)
+  std::vector<HSub> subs;      // its clustered subspaces
 };
 
 // One result-map entry (a clustered subspace) during the commit.
@@ -267,7 +284,7 @@ struct LoopVec {
 // The clusters numbered in one dim loop (the reference's shared clustering
 // vector): label l -> component, and its size.
 struct LoopState {
-  std::vector<LabelRef> ref{LabelRef{-1, -1}};
+  std::vector<LabelRef> ref{LabelRef{nullptr, -1}};
   std::vector<int> size{0};
   int nlabels = 0;
 };
@@ -441,10 +458,12 @@ class Engine {
   }
 
   // commit
-  void replay(int ci);
-  bool prune_redundancy(const HCall& c, uint64_t smask);
+  void replay_root(int D);
+  void replay(const Phase& ph, int ci);
+  const HLevel& level_of(const Phase& ph, const HCall& c) const { return c.level == 1 ? level1_ : ph.levels[c.level]; }
+  bool prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask);
   const std::vector<int>& superset_candidates(uint64_t smask);
-  void cluster_into(const HCall& c, LoopVec& V, LoopState& st);
+  void cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState& st);
   void join(LoopVec& V, LoopState& st, uint64_t smask);
   void split_pieces(long long work);
 
@@ -457,9 +476,10 @@ class Engine {
   HostParams hp_;
   long long n_ = 0;
   int d_ = 0;
-  std::vector<HCall> calls_;
-  std::vector<HLevel> levels_;
-  std::vector<HSub> subs_;
+  HCall root_;                 // the root call (all points, nothing restricted)
+  HLevel level1_;              // points and component orders of the level-1 calls
+  std::vector<Phase> phases_;  // ranges of first restricted dims
+  std::vector<int> phase_of_;  // phase of every first restricted dim
   std::vector<std::unique_ptr<Entry>> ents_;  // result map entries, in insertion order
   std::vector<uint64_t> emask_;               // their subspaces
   std::map<uint64_t, int> eidx_;              // subspace -> entry
@@ -483,9 +503,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   hp_ = hp;
   n_ = n;
   d_ = d;
-  calls_.clear();
-  levels_.clear();
-  subs_.clear();
+  root_ = HCall();
+  level1_ = HLevel();
+  phases_.clear();
+  phase_of_.clear();
   ents_.clear();
   emask_.clear();
   eidx_.clear();
@@ -649,572 +670,646 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   stats_.ms_setup = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup0).count();
 
   // ------------------------------------------------------------ expansion
-  // current calls (device descriptors + host records)
-  std::vector<CallDesc> hcalls(1);
-  hcalls[0].pts_off = 0;
-  hcalls[0].ghost_off = 0;
-  hcalls[0].rmask = 0;
-  hcalls[0].npts = ni;
-  hcalls[0].f = 0;
-  hcalls[0].nghost = 0;
-  hcalls[0].sub = -1;
-  hcalls[0].child_sub = 0;
-  hcalls[0].nrestricted = 0;
-  std::vector<int> call_ids(1, 0);
-  calls_.push_back(HCall());
-  calls_[0].npts = ni;
-  levels_.push_back(HLevel());
-
-  std::unique_ptr<Scope> cur_pts(new Scope(*pool_, s));  // the current calls' points and ghosts
-  int* d_pts = droot;
-  int2* d_ghosts = cur_pts->get<int2>(1);
-
-  struct PrevLevel {
-    std::unique_ptr<Scope> mem;
-    std::vector<SubDesc> subs;
-    std::vector<long long> kstart;  // nsubs + 1
+  // The frontier of the expansion: the calls of one level (device
+  // descriptors and the index of their host record) and what the next level
+  // needs from this one.
+  struct Frontier {
+    int level = 0;
+    std::vector<CallDesc> hcalls;
+    std::vector<int> call_ids;       // host record of each call in its phase; -1: the root
+    std::shared_ptr<Scope> pts_mem;  // the calls' points and detached chains
+    int* d_pts = nullptr;
+    int2* d_ghosts = nullptr;
+    long long pts_total = 0, ghosts_total = 0;
+    std::shared_ptr<Scope> prev_mem;     // this level's kept lists
+    std::vector<long long> prev_kstart;  // kept-index start of every subspace of the level (+ the total)
     int* keep_ids = nullptr;
     long long* keep_loff = nullptr;
     int* keep_lcnt = nullptr;
     int* lids = nullptr;
     float* lacc = nullptr;
-    long long total = 0;  // list entries
-    long long nkeep = 0;  // kept points
-  } prev;
-  long long pts_in_total = n, ghosts_in_total = 0;
-
-  int level = 0;
-  while (!hcalls.empty()) {
-    ++level;
-    stats_.levels = level;
-    Scope lv(*pool_, s);  // this level's temporaries
-    std::unique_ptr<Scope> keepmem(new Scope(*pool_, s));  // this level's kept lists (live one more level)
-
-    // ---- 1. subspaces of this level: children of the calls' subspaces
-    std::vector<SubDesc> subs;
-    std::map<int, int> child_base;  // parent subspace -> first child
-    for (auto& c : hcalls) {
-      auto it = child_base.find(c.sub);
-      if (it == child_base.end()) {
-        int base = (int)subs.size();
-        child_base[c.sub] = base;
-        uint64_t pm = c.rmask;
-        int first = c.f;
-        long long nq = c.sub < 0 ? n : prev.kstart[c.sub + 1] - prev.kstart[c.sub];
-        long long qo = c.sub < 0 ? 0 : prev.kstart[c.sub];
-        for (int D = first; D < d; ++D) {
-          SubDesc S;
-          S.mask = pm | (1ull << D);
-          S.dim = D;
-          S.nsub = __builtin_popcountll(S.mask);
-          S.parent = c.sub;
-          S.nquery = (int)nq;
-          S.item_off = 0;
-          S.query_off = qo;
-          S.plist_base = 0;
-          S.bitmap_off = 0;
-          subs.push_back(S);
-        }
-        c.child_sub = base;
-      } else {
-        c.child_sub = it->second;
-      }
-    }
-    const int nsubs = (int)subs.size();
-    long long nitems = 0;
-    for (int i = 0; i < nsubs; ++i) {
-      subs[i].item_off = nitems;
-      subs[i].bitmap_off = (long long)i * 3 * W;
-      nitems += subs[i].nquery;
-    }
-    stats_.subspaces += nsubs;
-    SubDesc* dsubs = lv.get<SubDesc>(nsubs);
-    h2d(dsubs, subs.data(), sizeof(SubDesc) * nsubs, s);
-
-    // groups: the children of one parent subspace, walked child-fastest
-    std::vector<GroupDesc> groups;
-    long long ngroup_warps = 0;  // one warp per (group, query point)
-    {
-      long long wo = 0;
-      for (int i = 0; i < nsubs;) {
-        int j = i;
-        while (j < nsubs && subs[j].parent == subs[i].parent) ++j;
-        GroupDesc g;
-        g.warp_off = wo;
-        g.qwarp_off = ngroup_warps;
-        g.sub_base = i;
-        g.nchild = j - i;
-        g.nquery = subs[i].nquery;
-        g.pad = 0;
-        wo += (long long)g.nchild * g.nquery;
-        ngroup_warps += g.nquery;
-        groups.push_back(g);
-        i = j;
-      }
-      if (wo != nitems) throw Error(INSCY_ERR_INTERNAL, "work item count mismatch");
-    }
-    GroupDesc* dgroups = lv.get<GroupDesc>(groups.size());
-    h2d(dgroups, groups.data(), sizeof(GroupDesc) * groups.size(), s);
-
-    // ---- 2. neighbour counts of every (subspace, point)
-    int* dcnt = lv.get<int>(nitems);
-    uint8_t* dflags = lv.get<uint8_t>(nitems);
-    unsigned* dbm = keepmem->get<unsigned>((size_t)nsubs * 3 * W);
-    CK(cudaMemsetAsync(dbm, 0, sizeof(unsigned) * (size_t)nsubs * 3 * W, s));
-    DensityLaunch DL;
-    std::memset(&DL, 0, sizeof(DL));
-    DL.subs = dsubs;
-    DL.nsubs = nsubs;
-    DL.nitems = nitems;
-    DL.groups = dgroups;
-    DL.ngroups = (int)groups.size();
-    DL.X = dX;
-    DL.fc = dfc;
-    DL.n = ni;
-    DL.d = d;
-    DL.G = G;
-    DL.eps = hp.eps;
-    DL.rect = hp.rect;
-    DL.acc_max = acc_max;
-    DL.thr_weak = thr_weak;
-    DL.thr_dense = dthr;
-    DL.thr_keep = dthr + d + 2;
-    DL.cand_off = dcoff;
-    DL.cand_pts = dcand;
-    DL.prev_keep = prev.keep_ids;
-    DL.prev_loff = prev.keep_loff;
-    DL.prev_lcnt = prev.keep_lcnt;
-    DL.prev_lids = prev.lids;
-    DL.prev_lacc = prev.lacc;
-    DL.cnt = dcnt;
-    DL.flags = dflags;
-    DL.bitmaps = dbm;
-    DL.words = W;
-    DL.prev_total = prev.total;
-    DL.prev_nkeep = prev.nkeep;
-    DL.total = 0;
-    DL.guard = guard;
-    unsigned long long* dcand_cnt = lv.get<unsigned long long>(2);
-    CK(cudaMemsetAsync(dcand_cnt, 0, 2 * sizeof(unsigned long long), s));
-    DL.cand_counter = dcand_cnt;
-    DL.list_counter = dcand_cnt + 1;
-    auto neighbours = [&](bool write) {
-      if (level == 1)
-        launch_neighbours(DL, write, s);
-      else
-        launch_neighbours_multi(DL, ngroup_warps, write, s);
-    };
-    double ms1 = timed(s, [&] { neighbours(false); });
-    stats_.ms_density += ms1;
-    stats_.ms_density_pass1 += ms1;
-    stats_.density_launches_pass1 += 1;
-    ++launches;
-    {
-      // algorithmic bytes of the count pass: per (subspace, point) 26 B (its
-      // id, list offset and length, own coordinate and fine cell, count out);
-      // per list entry read 8 B (id + partial distance; at level 1 id +
-      // coordinate); per further (candidate, child subspace) test at levels
-      // >= 2 5 B (the candidate's coordinate and fine cell on that dim)
-      unsigned long long nc[2];
-      d2h(nc, dcand_cnt, sizeof(nc), s);
-      stats_.candidates += (long long)nc[0];
-      stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] + (level == 1 ? 0.0 : 5.0 * (double)nc[0]);
-    }
-    check_guard("density count");  // the counts size every later buffer
-    DL.cand_counter = nullptr;
-    DL.list_counter = nullptr;
-
-    // ---- 3. ordered lists of every item, then densities and flags
-    long long* dloff = lv.get<long long>(nitems);
-    long long* dtot = lv.get<long long>(2);
-    void* sums = scan_sums(std::max(nitems, (long long)nsubs * W) + 1, s, lv);
-    launch_exclusive_scan_i2ll(dcnt, dloff, nitems, dtot, sums, s);
-    launches += 3;
-    const long long L = scalar(dtot, s);
-    int* lids = keepmem->get<int>(L);
-    float* lacc = keepmem->get<float>(L);
-    DL.loff = dloff;
-    DL.lids = lids;
-    DL.lacc = lacc;
-    DL.total = L;
-    stats_.ms_density += timed(s, [&] {
-      neighbours(true);
-      launch_density_flags(DL, s);
-    });
-    launches += 2;
-    // kept items
-    int* dkcnt = lv.get<int>(nitems);
-    int* dkflag = lv.get<int>(nitems);
-    long long* dkpos = lv.get<long long>(nitems + 1);
-    launch_keep_counts(dcnt, dflags, nitems, dkcnt, dkflag, s);
-    launch_exclusive_scan_i2ll(dkflag, dkpos, nitems, dtot + 1, sums, s);
-    launches += 4;
-    const long long K = scalar(dtot + 1, s);
-    check_guard("density");
-    int* keep_ids = keepmem->get<int>(K);
-    long long* keep_loff = keepmem->get<long long>(K);
-    int* keep_lcnt = keepmem->get<int>(K);
-    launch_keep_compact(dsubs, nsubs, nitems, dflags, dcnt, dkpos, dloff, prev.keep_ids, keep_ids, keep_loff,
-                        keep_lcnt, s);
-    launches += 2;
-    // kept-index start of every subspace
-    long long* dkstart = keepmem->get<long long>(nsubs + 1);
-    launch_gather_kstart(dsubs, nsubs, dkpos, nitems, K, dkstart, s);
-    ++launches;
-    std::vector<long long> kstart(nsubs + 1);
-    d2h(kstart.data(), dkstart, sizeof(long long) * (nsubs + 1), s);
-    // global rank of every kept bit: prefix of the kept-bitmap popcounts
-    int* dkwr = keepmem->get<int>((size_t)nsubs * W + 1);
-    {
-      int* pc = lv.get<int>((size_t)nsubs * W + 1);
-      launch_keep_popc(dbm, nsubs, W, pc, s);
-      ++launches;
-      int* dt = lv.get<int>(1);
-      launch_exclusive_scan_int(pc, dkwr, (long long)nsubs * W, dt, sums, s);
-      launches += 3;
-    }
-
-    // ---- 4. restrict / merge / prune of every (call, dim)
-    const int ncalls = (int)hcalls.size();
-    std::vector<long long> work_off(ncalls), work_scr;
-    long long nwork = 0, scr = 0, pts_cap = 0, ghost_in = 0;
-    for (int i = 0; i < ncalls; ++i) {
-      work_off[i] = nwork;
-      int nd = d - hcalls[i].f;
-      for (int t = 0; t < nd; ++t) {
-        work_scr.push_back(scr);
-        // keys (16 B) of points and chains, then ints (see k_tree_level)
-        long long bytes = 16LL * (2LL * hcalls[i].npts + 2LL * hcalls[i].nghost) +
-                          4LL * (3LL * hcalls[i].npts + 1 + 2LL * hcalls[i].nghost);
-        scr += (bytes + 15) / 16 * 16;
-      }
-      nwork += nd;
-      pts_cap += (long long)hcalls[i].npts * nd;
-      ghost_in += (long long)hcalls[i].nghost * nd;
-    }
-    stats_.regions += 0;
-    CallDesc* dcalls = lv.get<CallDesc>(ncalls);
-    h2d(dcalls, hcalls.data(), sizeof(CallDesc) * ncalls, s);
-    long long* dwork = lv.get<long long>(ncalls);
-    h2d(dwork, work_off.data(), sizeof(long long) * ncalls, s);
-    long long* dwscr = lv.get<long long>(nwork);
-    h2d(dwscr, work_scr.data(), sizeof(long long) * nwork, s);
-    char* dscr = lv.get<char>(scr);
-    RegionRec* drecs = lv.get<RegionRec>((size_t)nwork * cells);
-    int* dnrecs = lv.get<int>(nwork);
-    std::unique_ptr<Scope> next_pts(new Scope(*pool_, s));
-    int* dout_pts = next_pts->get<int>(pts_cap);
-    unsigned long long* dtops = lv.get<unsigned long long>(2);
-    int* derr = lv.get<int>(1);
-    long long ghost_cap = std::max(1024LL, ghost_in + 2 * pts_cap);
-    int2* dout_gh = nullptr;
-    std::vector<RegionRec> recs;
-    std::vector<int> nrecs(nwork);
-    unsigned long long tops[2];
-    for (int attempt = 0;; ++attempt) {
-      dout_gh = next_pts->get<int2>(ghost_cap);
-      CK(cudaMemsetAsync(dtops, 0, sizeof(unsigned long long) * 2, s));
-      CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
-      TreeLaunch TL;
-      TL.calls = dcalls;
-      TL.ncalls = ncalls;
-      TL.work_off = dwork;
-      TL.nwork = (int)nwork;
-      TL.pts_in = d_pts;
-      TL.ghosts_in = d_ghosts;
-      TL.cc = dcc;
-      TL.gz = dgz;
-      TL.n = ni;
-      TL.d = d;
-      TL.cells = cells;
-      TL.min_size = hp.min_size;
-      TL.kbits = kbits;
-      TL.subs = dsubs;
-      TL.bitmaps = dbm;
-      TL.scratch = dscr;
-      TL.work_scratch = dwscr;
-      TL.recs = drecs;
-      TL.nrecs = dnrecs;
-      TL.out_pts = dout_pts;
-      TL.out_pts_top = dtops;
-      TL.out_pts_cap = pts_cap;
-      TL.out_ghosts = dout_gh;
-      TL.out_ghost_top = dtops + 1;
-      TL.out_ghost_cap = ghost_cap;
-      TL.err = derr;
-      TL.pts_in_total = pts_in_total;
-      TL.ghosts_in_total = ghosts_in_total;
-      TL.guard = guard;
-      stats_.ms_tree += timed(s, [&] { launch_tree_level(TL, s); });
-      ++launches;
-      int err = scalar(derr, s);
-      d2h(tops, dtops, sizeof(tops), s);
-      if (err == 2 && attempt < 4) {
-        ghost_cap = (long long)tops[1] + 1024;
-        continue;
-      }
-      if (err) throw Error(INSCY_ERR_INTERNAL, "level kernel reported error " + std::to_string(err));
-      check_guard("restrict/merge/prune");
-      break;
-    }
-    recs.resize((size_t)nwork * cells);
-    d2h(recs.data(), drecs, sizeof(RegionRec) * recs.size(), s);
-    d2h(nrecs.data(), dnrecs, sizeof(int) * nwork, s);
-    stats_.tree_bytes += 0;
-
-    // ---- 5. next level's calls (host records in the reference's order)
-    std::vector<CallDesc> ncall;
-    std::vector<int> ncall_ids;
-    for (int i = 0; i < ncalls; ++i) {
-      HCall& parent = calls_[call_ids[i]];
-      int nd = d - hcalls[i].f;
-      for (int t = 0; t < nd; ++t) {
-        long long w = work_off[i] + t;
-        for (int r = 0; r < nrecs[w]; ++r) {
-          const RegionRec& R = recs[(size_t)w * cells + r];
-          stats_.regions++;
-          HRegion hr;
-          hr.dim = R.dim;
-          hr.passed = R.passed;
-          hr.child = -1;
-          if (R.passed) {
-            CallDesc c;
-            c.pts_off = R.pts_off;
-            c.ghost_off = R.ghost_off;
-            c.rmask = hcalls[i].rmask | (1ull << R.dim);
-            c.npts = R.npts;
-            c.f = R.dim + 1;
-            c.nghost = R.nghost;
-            c.sub = hcalls[i].child_sub + (R.dim - hcalls[i].f);
-            c.child_sub = 0;
-            c.nrestricted = hcalls[i].nrestricted + 1;
-            ncall.push_back(c);
-            HCall hc;
-            hc.rmask = c.rmask;
-            hc.f = c.f;
-            hc.level = level;
-            hc.npts = c.npts;
-            hc.pts_off = c.pts_off;
-            hr.child = (int)calls_.size();
-            ncall_ids.push_back(hr.child);
-            calls_.push_back(hc);
-          }
-          calls_[call_ids[i]].regions.push_back(hr);
-          (void)parent;
-        }
-      }
-    }
-    stats_.calls += (long long)ncall.size();
-
-    // ---- 6. clustering of the subspaces that gained calls
-    levels_.push_back(HLevel());
-    HLevel& hl = levels_.back();
-    if (!ncall.empty()) {
-      hl.pts.resize(tops[0]);
-      d2h(hl.pts.data(), dout_pts, sizeof(int) * tops[0], s);
-      std::vector<uint8_t> clustered(nsubs, 0);
-      std::vector<std::vector<int>> sub_calls(nsubs);
-      for (size_t j = 0; j < ncall.size(); ++j) {
-        clustered[ncall[j].sub] = 1;
-        sub_calls[ncall[j].sub].push_back((int)j);
-      }
-      std::vector<int> clist, cslot(nsubs, -1), sc_off(1, 0), sc_list;
-      for (int i = 0; i < nsubs; ++i)
-        if (clustered[i]) {
-          cslot[i] = (int)clist.size();
-          clist.push_back(i);
-          for (int j : sub_calls[i]) sc_list.push_back(j);
-          sc_off.push_back((int)sc_list.size());
-        }
-      const int ncl = (int)clist.size();
-      uint8_t* dcl = lv.get<uint8_t>(nsubs);
-      h2d(dcl, clustered.data(), nsubs, s);
-      int* dclist = lv.get<int>(ncl);
-      h2d(dclist, clist.data(), sizeof(int) * ncl, s);
-      int* dcslot = lv.get<int>(nsubs);
-      h2d(dcslot, cslot.data(), sizeof(int) * nsubs, s);
-      int* dscoff = lv.get<int>(sc_off.size());
-      h2d(dscoff, sc_off.data(), sizeof(int) * sc_off.size(), s);
-      int* dsclist = lv.get<int>(sc_list.size());
-      h2d(dsclist, sc_list.data(), sizeof(int) * sc_list.size(), s);
-      CallDesc* dncall = lv.get<CallDesc>(ncall.size());
-      h2d(dncall, ncall.data(), sizeof(CallDesc) * ncall.size(), s);
-
-      ClusterArgs CA;
-      CA.nsubs = nsubs;
-      CA.subs = dsubs;
-      CA.kstart = dkstart;
-      CA.keep_ids = keep_ids;
-      CA.keep_loff = keep_loff;
-      CA.keep_lcnt = keep_lcnt;
-      CA.lids = lids;
-      CA.bitmaps = dbm;
-      CA.words = W;
-      CA.keep_word_rank = dkwr;
-      CA.clustered = dcl;
-      CA.clustered_list = dclist;
-      CA.nkeep = K;
-      CA.n = ni;
-      CA.uf = lv.get<int>(K + 1);
-      CA.err = derr;
-      CA.guard = guard;
-      CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
-      int* is_root = lv.get<int>(K + 1);
-      int* root_id = lv.get<int>(K + 1);
-      int* comp = lv.get<int>(K + 1);
-      int* root_of = lv.get<int>(K + 1);
-      int* dsample = lv.get<int>(ncl + 1);
-      int* dnc = lv.get<int>(1);
-      long long ncomp = 0;
-      std::vector<int> cbase(nsubs + 1);
-      stats_.ms_cluster += timed(s, [&] {
-        launch_uf_init(CA.uf, K, s);
-        launch_uf_union(CA, ncl, dcslot, dsample, s);
-        launch_uf_flatten(CA, is_root, root_of, s);
-        launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
-      });
-      launches += 8;
-      ncomp = scalar(dnc, s);
-      int* dcbase = lv.get<int>(nsubs + 1);
-      launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);
-      ++launches;
-      d2h(cbase.data(), dcbase, sizeof(int) * (nsubs + 1), s);
-      int* mcount = lv.get<int>(ncomp + 1);
-      int* mfill = lv.get<int>(ncomp + 1);
-      long long* moff = lv.get<long long>(ncomp + 1);
-      int* bcount = lv.get<int>(ncomp + 1);
-      int* bfill = lv.get<int>(ncomp + 1);
-      long long* boff = lv.get<long long>(ncomp + 1);
-      CK(cudaMemsetAsync(mcount, 0, sizeof(int) * (ncomp + 1), s));
-      CK(cudaMemsetAsync(mfill, 0, sizeof(int) * (ncomp + 1), s));
-      CK(cudaMemsetAsync(bcount, 0, sizeof(int) * (ncomp + 1), s));
-      CK(cudaMemsetAsync(bfill, 0, sizeof(int) * (ncomp + 1), s));
-      long long nslots2 = (long long)ncl * n * 2;
-      int* slots = lv.get<int>(nslots2);
-      CK(cudaMemsetAsync(slots, 0xff, sizeof(int) * nslots2, s));
-      const int ovf_cap = 1 << 20;
-      int2* ovf = lv.get<int2>(ovf_cap);
-      int* novf = lv.get<int>(1);
-      CK(cudaMemsetAsync(novf, 0, sizeof(int), s));
-      long long* dmtot = lv.get<long long>(2);
-      stats_.ms_cluster += timed(s, [&] {
-        launch_comp_ids(CA, root_id, root_of, comp, mcount, s);
-        launch_exclusive_scan_i2ll(mcount, moff, ncomp, dmtot, sums, s);
-      });
-      launches += 4;
-      long long hm[2];
-      d2h(hm, dmtot, sizeof(long long), s);
-      int* members = lv.get<int>(hm[0] + 1);
-      launch_members(CA, comp, moff, mfill, members, s);
-      launches += 1;
-      int hovf = 0;
-      stats_.ms_cluster += timed(s, [&] { launch_borders(CA, comp, dcslot, slots, ovf, novf, ovf_cap, s); });
-      launches += 1;
-      hovf = scalar(novf, s);
-      if (scalar(derr, s)) throw Error(INSCY_ERR_INTERNAL, "clustering kernels reported an error");
-      check_guard("clustering");
-      hovf = std::min(hovf, ovf_cap);
-      launch_border_count(slots, nslots2, ovf, hovf, bcount, s);
-      launch_exclusive_scan_i2ll(bcount, boff, ncomp, dmtot + 1, sums, s);
-      launches += 5;
-      long long hb;
-      d2h(&hb, dmtot + 1, sizeof(long long), s);
-      int* borders = lv.get<int>(hb + 1);
-      launch_border_fill(slots, nslots2, ni, ovf, hovf, boff, bfill, borders, s);
-      // components of each region in first-seed order
-      int* firstpos = lv.get<int>(ncomp + 1);
-      CK(cudaMemsetAsync(firstpos, 0x7f, sizeof(int) * (ncomp + 1), s));
-      int* order = lv.get<int>(tops[0] + 1);
-      int* order_cnt = lv.get<int>(ncall.size());
-      stats_.ms_cluster += timed(s, [&] {
-        launch_region_order(CA, ncl, comp, dcbase, dscoff, dsclist, dncall, dout_pts, firstpos, order, order_cnt, s);
-      });
-      launches += 3;
-      // to the host
-      std::vector<long long> hmoff(ncomp + 1), hboff(ncomp + 1);
-      d2h(hmoff.data(), moff, sizeof(long long) * ncomp, s);
-      hmoff[ncomp] = hm[0];
-      d2h(hboff.data(), boff, sizeof(long long) * ncomp, s);
-      hboff[ncomp] = hb;
-      std::vector<int> hmem(hm[0]), hbor(hb);
-      d2h(hmem.data(), members, sizeof(int) * hm[0], s);
-      d2h(hbor.data(), borders, sizeof(int) * hb, s);
-      std::vector<int> hocnt(ncall.size());
-      long long* order_off = lv.get<long long>(ncall.size() + 1);
-      long long* dot = lv.get<long long>(1);
-      launch_exclusive_scan_i2ll(order_cnt, order_off, (long long)ncall.size(), dot,
-                                 scan_sums((long long)ncall.size() + 1, s, lv), s);
-      const long long norder_tot = scalar(dot, s);
-      int* packed = lv.get<int>(norder_tot + 1);
-      launch_pack_order(dncall, (int)ncall.size(), order, order_cnt, order_off, packed, s);
-      launches += 4;
-      hl.order.resize(norder_tot);
-      d2h(hl.order.data(), packed, sizeof(int) * norder_tot, s);
-      check_guard("component order");
-      d2h(hocnt.data(), order_cnt, sizeof(int) * ncall.size(), s);
-      std::vector<long long> hooff(ncall.size());
-      d2h(hooff.data(), order_off, sizeof(long long) * ncall.size(), s);
-      // one HSub per clustered subspace (component-local offsets)
-      std::vector<int> csub_of(nsubs, -1);
-      for (int i : clist) {
-        HSub hs;
-        long long c0 = cbase[i], c1 = cbase[i + 1];
-        hs.moff.resize(c1 - c0 + 1);
-        hs.boff.resize(c1 - c0 + 1);
-        for (long long c = c0; c <= c1; ++c) {
-          hs.moff[c - c0] = hmoff[c] - hmoff[c0];
-          hs.boff[c - c0] = hboff[c] - hboff[c0];
-        }
-        hs.members.assign(hmem.begin() + hmoff[c0], hmem.begin() + hmoff[c1]);
-        hs.borders.assign(hbor.begin() + hboff[c0], hbor.begin() + hboff[c1]);
-        csub_of[i] = (int)subs_.size();
-        subs_.push_back(std::move(hs));
-      }
-      for (size_t j = 0; j < ncall.size(); ++j) {
-        HCall& hc = calls_[ncall_ids[j]];
-        hc.csub = csub_of[ncall[j].sub];
-        hc.norder = hocnt[j];
-        hc.order_off = hooff[j];
-      }
-    }
-
-    // ---- 7. advance: this level's lists become the parent lists
-    prev.mem = std::move(keepmem);
-    prev.subs = subs;
-    prev.kstart = kstart;
-    prev.keep_ids = keep_ids;
-    prev.keep_loff = keep_loff;
-    prev.keep_lcnt = keep_lcnt;
-    prev.lids = lids;
-    prev.lacc = lacc;
-    prev.total = L;
-    prev.nkeep = K;
-    pts_in_total = (long long)tops[0];
-    ghosts_in_total = (long long)tops[1];
-    cur_pts = std::move(next_pts);
-    d_pts = dout_pts;
-    d_ghosts = dout_gh;
-    hcalls.swap(ncall);
-    call_ids.swap(ncall_ids);
-    lv.release();
-    stats_.kernel_launches = launches;
+    long long prev_total = 0;  // list entries
+    long long prev_nkeep = 0;  // kept points
+  };
+  root_.npts = ni;
+  phase_of_.assign(d, 0);
+  for (int k = 0, d0 = 0; d0 < d; ++k) {
+    Phase ph;
+    ph.d0 = d0;
+    ph.d1 = std::min(d, 2 * d0 + 1);
+    for (int D = ph.d0; D < ph.d1; ++D) phase_of_[D] = k;
+    d0 = ph.d1;
+    phases_.push_back(std::move(ph));
   }
-  prev.mem.reset();
-  cur_pts.reset();
-  persist.release();
-  CK(cudaStreamSynchronize(s));
+  const int nphases = (int)phases_.size();
+  Frontier F1;
+  {
+    CallDesc c;
+    c.pts_off = 0;
+    c.ghost_off = 0;
+    c.rmask = 0;
+    c.npts = ni;
+    c.f = 0;
+    c.nghost = 0;
+    c.sub = -1;
+    c.child_sub = 0;
+    c.nrestricted = 0;
+    F1.hcalls.push_back(c);
+    F1.call_ids.push_back(-1);
+    F1.pts_mem.reset(new Scope(*pool_, s));
+    F1.d_pts = droot;
+    F1.d_ghosts = F1.pts_mem->get<int2>(1);
+    F1.pts_total = n;
+  }
+
+  // Expands the frontier level by level (one level only for the root).  The
+  // host records go to `phase` (at the root level: to the phase of each dim).
+  auto expand = [&](int phase, Frontier& F, bool one_level) {
+    while (!F.hcalls.empty()) {
+      const int level = ++F.level;
+      stats_.levels = std::max<long long>(stats_.levels, level);
+      Scope lv(*pool_, s);  // this level's temporaries
+      std::unique_ptr<Scope> keepmem(new Scope(*pool_, s));  // this level's kept lists (live one more level)
+
+      // ---- 1. subspaces of this level: children of the calls' subspaces
+      std::vector<SubDesc> subs;
+      std::map<int, int> child_base;  // parent subspace -> first child
+      for (auto& c : F.hcalls) {
+        auto it = child_base.find(c.sub);
+        if (it == child_base.end()) {
+          int base = (int)subs.size();
+          child_base[c.sub] = base;
+          uint64_t pm = c.rmask;
+          int first = c.f;
+          long long nq = c.sub < 0 ? n : F.prev_kstart[c.sub + 1] - F.prev_kstart[c.sub];
+          long long qo = c.sub < 0 ? 0 : F.prev_kstart[c.sub];
+          for (int D = first; D < d; ++D) {
+            SubDesc S;
+            S.mask = pm | (1ull << D);
+            S.dim = D;
+            S.nsub = __builtin_popcountll(S.mask);
+            S.parent = c.sub;
+            S.nquery = (int)nq;
+            S.item_off = 0;
+            S.query_off = qo;
+            S.plist_base = 0;
+            S.bitmap_off = 0;
+            subs.push_back(S);
+          }
+          c.child_sub = base;
+        } else {
+          c.child_sub = it->second;
+        }
+      }
+      const int nsubs = (int)subs.size();
+      long long nitems = 0;
+      for (int i = 0; i < nsubs; ++i) {
+        subs[i].item_off = nitems;
+        subs[i].bitmap_off = (long long)i * 3 * W;
+        nitems += subs[i].nquery;
+      }
+      stats_.subspaces += nsubs;
+      SubDesc* dsubs = lv.get<SubDesc>(nsubs);
+      h2d(dsubs, subs.data(), sizeof(SubDesc) * nsubs, s);
+
+      // groups: the children of one parent subspace, walked child-fastest
+      std::vector<GroupDesc> groups;
+      long long ngroup_warps = 0;  // one warp per (group, query point)
+      {
+        long long wo = 0;
+        for (int i = 0; i < nsubs;) {
+          int j = i;
+          while (j < nsubs && subs[j].parent == subs[i].parent) ++j;
+          GroupDesc g;
+          g.warp_off = wo;
+          g.qwarp_off = ngroup_warps;
+          g.sub_base = i;
+          g.nchild = j - i;
+          g.nquery = subs[i].nquery;
+          g.pad = 0;
+          wo += (long long)g.nchild * g.nquery;
+          ngroup_warps += g.nquery;
+          groups.push_back(g);
+          i = j;
+        }
+        if (wo != nitems) throw Error(INSCY_ERR_INTERNAL, "work item count mismatch");
+      }
+      GroupDesc* dgroups = lv.get<GroupDesc>(groups.size());
+      h2d(dgroups, groups.data(), sizeof(GroupDesc) * groups.size(), s);
+
+      // ---- 2. neighbour counts of every (subspace, point)
+      int* dcnt = lv.get<int>(nitems);
+      uint8_t* dflags = lv.get<uint8_t>(nitems);
+      unsigned* dbm = keepmem->get<unsigned>((size_t)nsubs * 3 * W);
+      CK(cudaMemsetAsync(dbm, 0, sizeof(unsigned) * (size_t)nsubs * 3 * W, s));
+      DensityLaunch DL;
+      std::memset(&DL, 0, sizeof(DL));
+      DL.subs = dsubs;
+      DL.nsubs = nsubs;
+      DL.nitems = nitems;
+      DL.groups = dgroups;
+      DL.ngroups = (int)groups.size();
+      DL.X = dX;
+      DL.fc = dfc;
+      DL.n = ni;
+      DL.d = d;
+      DL.G = G;
+      DL.eps = hp.eps;
+      DL.rect = hp.rect;
+      DL.acc_max = acc_max;
+      DL.thr_weak = thr_weak;
+      DL.thr_dense = dthr;
+      DL.thr_keep = dthr + d + 2;
+      DL.cand_off = dcoff;
+      DL.cand_pts = dcand;
+      DL.prev_keep = F.keep_ids;
+      DL.prev_loff = F.keep_loff;
+      DL.prev_lcnt = F.keep_lcnt;
+      DL.prev_lids = F.lids;
+      DL.prev_lacc = F.lacc;
+      DL.cnt = dcnt;
+      DL.flags = dflags;
+      DL.bitmaps = dbm;
+      DL.words = W;
+      DL.prev_total = F.prev_total;
+      DL.prev_nkeep = F.prev_nkeep;
+      DL.total = 0;
+      DL.guard = guard;
+      unsigned long long* dcand_cnt = lv.get<unsigned long long>(2);
+      CK(cudaMemsetAsync(dcand_cnt, 0, 2 * sizeof(unsigned long long), s));
+      DL.cand_counter = dcand_cnt;
+      DL.list_counter = dcand_cnt + 1;
+      auto neighbours = [&](bool write) {
+        if (level == 1)
+          launch_neighbours(DL, write, s);
+        else
+          launch_neighbours_multi(DL, ngroup_warps, write, s);
+      };
+      double ms1 = timed(s, [&] { neighbours(false); });
+      stats_.ms_density += ms1;
+      stats_.ms_density_pass1 += ms1;
+      stats_.density_launches_pass1 += 1;
+      ++launches;
+      {
+        // algorithmic bytes of the count pass: per (subspace, point) 26 B (its
+        // id, list offset and length, own coordinate and fine cell, count out);
+        // per list entry read 8 B (id + partial distance; at level 1 id +
+        // coordinate); per further (candidate, child subspace) test at levels
+        // >= 2 5 B (the candidate's coordinate and fine cell on that dim)
+        unsigned long long nc[2];
+        d2h(nc, dcand_cnt, sizeof(nc), s);
+        stats_.candidates += (long long)nc[0];
+        stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] + (level == 1 ? 0.0 : 5.0 * (double)nc[0]);
+      }
+      check_guard("density count");  // the counts size every later buffer
+      DL.cand_counter = nullptr;
+      DL.list_counter = nullptr;
+
+      // ---- 3. ordered lists of every item, then densities and flags
+      long long* dloff = lv.get<long long>(nitems);
+      long long* dtot = lv.get<long long>(2);
+      void* sums = scan_sums(std::max(nitems, (long long)nsubs * W) + 1, s, lv);
+      launch_exclusive_scan_i2ll(dcnt, dloff, nitems, dtot, sums, s);
+      launches += 3;
+      const long long L = scalar(dtot, s);
+      int* lids = keepmem->get<int>(L);
+      float* lacc = keepmem->get<float>(L);
+      DL.loff = dloff;
+      DL.lids = lids;
+      DL.lacc = lacc;
+      DL.total = L;
+      stats_.ms_density += timed(s, [&] {
+        neighbours(true);
+        launch_density_flags(DL, s);
+      });
+      launches += 2;
+      // kept items
+      int* dkcnt = lv.get<int>(nitems);
+      int* dkflag = lv.get<int>(nitems);
+      long long* dkpos = lv.get<long long>(nitems + 1);
+      launch_keep_counts(dcnt, dflags, nitems, dkcnt, dkflag, s);
+      launch_exclusive_scan_i2ll(dkflag, dkpos, nitems, dtot + 1, sums, s);
+      launches += 4;
+      const long long K = scalar(dtot + 1, s);
+      check_guard("density");
+      int* keep_ids = keepmem->get<int>(K);
+      long long* keep_loff = keepmem->get<long long>(K);
+      int* keep_lcnt = keepmem->get<int>(K);
+      launch_keep_compact(dsubs, nsubs, nitems, dflags, dcnt, dkpos, dloff, F.keep_ids, keep_ids, keep_loff,
+                          keep_lcnt, s);
+      launches += 2;
+      // kept-index start of every subspace
+      long long* dkstart = keepmem->get<long long>(nsubs + 1);
+      launch_gather_kstart(dsubs, nsubs, dkpos, nitems, K, dkstart, s);
+      ++launches;
+      std::vector<long long> kstart(nsubs + 1);
+      d2h(kstart.data(), dkstart, sizeof(long long) * (nsubs + 1), s);
+      // global rank of every kept bit: prefix of the kept-bitmap popcounts
+      int* dkwr = keepmem->get<int>((size_t)nsubs * W + 1);
+      {
+        int* pc = lv.get<int>((size_t)nsubs * W + 1);
+        launch_keep_popc(dbm, nsubs, W, pc, s);
+        ++launches;
+        int* dt = lv.get<int>(1);
+        launch_exclusive_scan_int(pc, dkwr, (long long)nsubs * W, dt, sums, s);
+        launches += 3;
+      }
+
+      // ---- 4. restrict / merge / prune of every (call, dim)
+      const int ncalls = (int)F.hcalls.size();
+      std::vector<long long> work_off(ncalls), work_scr;
+      long long nwork = 0, scr = 0, pts_cap = 0, ghost_in = 0;
+      for (int i = 0; i < ncalls; ++i) {
+        work_off[i] = nwork;
+        int nd = d - F.hcalls[i].f;
+        for (int t = 0; t < nd; ++t) {
+          work_scr.push_back(scr);
+          // keys (16 B) of points and chains, then ints (see k_tree_level)
+          long long bytes = 16LL * (2LL * F.hcalls[i].npts + 2LL * F.hcalls[i].nghost) +
+                            4LL * (3LL * F.hcalls[i].npts + 1 + 2LL * F.hcalls[i].nghost);
+          scr += (bytes + 15) / 16 * 16;
+        }
+        nwork += nd;
+        pts_cap += (long long)F.hcalls[i].npts * nd;
+        ghost_in += (long long)F.hcalls[i].nghost * nd;
+      }
+      stats_.regions += 0;
+      CallDesc* dcalls = lv.get<CallDesc>(ncalls);
+      h2d(dcalls, F.hcalls.data(), sizeof(CallDesc) * ncalls, s);
+      long long* dwork = lv.get<long long>(ncalls);
+      h2d(dwork, work_off.data(), sizeof(long long) * ncalls, s);
+      long long* dwscr = lv.get<long long>(nwork);
+      h2d(dwscr, work_scr.data(), sizeof(long long) * nwork, s);
+      char* dscr = lv.get<char>(scr);
+      RegionRec* drecs = lv.get<RegionRec>((size_t)nwork * cells);
+      int* dnrecs = lv.get<int>(nwork);
+      std::unique_ptr<Scope> next_pts(new Scope(*pool_, s));
+      int* dout_pts = next_pts->get<int>(pts_cap);
+      unsigned long long* dtops = lv.get<unsigned long long>(2);
+      int* derr = lv.get<int>(1);
+      long long ghost_cap = std::max(1024LL, ghost_in + 2 * pts_cap);
+      int2* dout_gh = nullptr;
+      std::vector<RegionRec> recs;
+      std::vector<int> nrecs(nwork);
+      unsigned long long tops[2];
+      for (int attempt = 0;; ++attempt) {
+        dout_gh = next_pts->get<int2>(ghost_cap);
+        CK(cudaMemsetAsync(dtops, 0, sizeof(unsigned long long) * 2, s));
+        CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
+        TreeLaunch TL;
+        TL.calls = dcalls;
+        TL.ncalls = ncalls;
+        TL.work_off = dwork;
+        TL.nwork = (int)nwork;
+        TL.pts_in = F.d_pts;
+        TL.ghosts_in = F.d_ghosts;
+        TL.cc = dcc;
+        TL.gz = dgz;
+        TL.n = ni;
+        TL.d = d;
+        TL.cells = cells;
+        TL.min_size = hp.min_size;
+        TL.kbits = kbits;
+        TL.subs = dsubs;
+        TL.bitmaps = dbm;
+        TL.scratch = dscr;
+        TL.work_scratch = dwscr;
+        TL.recs = drecs;
+        TL.nrecs = dnrecs;
+        TL.out_pts = dout_pts;
+        TL.out_pts_top = dtops;
+        TL.out_pts_cap = pts_cap;
+        TL.out_ghosts = dout_gh;
+        TL.out_ghost_top = dtops + 1;
+        TL.out_ghost_cap = ghost_cap;
+        TL.err = derr;
+        TL.pts_in_total = F.pts_total;
+        TL.ghosts_in_total = F.ghosts_total;
+        TL.guard = guard;
+        stats_.ms_tree += timed(s, [&] { launch_tree_level(TL, s); });
+        ++launches;
+        int err = scalar(derr, s);
+        d2h(tops, dtops, sizeof(tops), s);
+        if (err == 2 && attempt < 4) {
+          ghost_cap = (long long)tops[1] + 1024;
+          continue;
+        }
+        if (err) throw Error(INSCY_ERR_INTERNAL, "level kernel reported error " + std::to_string(err));
+        check_guard("restrict/merge/prune");
+        break;
+      }
+      recs.resize((size_t)nwork * cells);
+      d2h(recs.data(), drecs, sizeof(RegionRec) * recs.size(), s);
+      d2h(nrecs.data(), dnrecs, sizeof(int) * nwork, s);
+      stats_.tree_bytes += 0;
+
+      // ---- 5. next level's calls (host records in the reference's order)
+      std::vector<CallDesc> ncall;
+      std::vector<int> ncall_ids, ncall_phase;
+      for (int i = 0; i < ncalls; ++i) {
+        int nd = d - F.hcalls[i].f;
+        for (int t = 0; t < nd; ++t) {
+          long long w = work_off[i] + t;
+          for (int r = 0; r < nrecs[w]; ++r) {
+            const RegionRec& R = recs[(size_t)w * cells + r];
+            stats_.regions++;
+            HRegion hr;
+            hr.dim = R.dim;
+            hr.passed = R.passed;
+            hr.child = -1;
+            if (R.passed) {
+              CallDesc c;
+              c.pts_off = R.pts_off;
+              c.ghost_off = R.ghost_off;
+              c.rmask = F.hcalls[i].rmask | (1ull << R.dim);
+              c.npts = R.npts;
+              c.f = R.dim + 1;
+              c.nghost = R.nghost;
+              c.sub = F.hcalls[i].child_sub + (R.dim - F.hcalls[i].f);
+              c.child_sub = 0;
+              c.nrestricted = F.hcalls[i].nrestricted + 1;
+              ncall.push_back(c);
+              HCall hc;
+              hc.rmask = c.rmask;
+              hc.f = c.f;
+              hc.level = level;
+              hc.npts = c.npts;
+              hc.pts_off = c.pts_off;
+              const int cp = phase < 0 ? phase_of_[R.dim] : phase;  // the root's restrictions start the phases
+              hr.child = (int)phases_[cp].calls.size();
+              ncall_ids.push_back(hr.child);
+              ncall_phase.push_back(cp);
+              phases_[cp].calls.push_back(hc);
+            }
+            (F.call_ids[i] < 0 ? root_ : phases_[phase].calls[F.call_ids[i]]).regions.push_back(hr);
+          }
+        }
+      }
+      stats_.calls += (long long)ncall.size();
+
+      // ---- 6. clustering of the subspaces that gained calls
+      if (phase >= 0 && (int)phases_[phase].levels.size() <= level) phases_[phase].levels.resize(level + 1);
+      HLevel& hl = phase < 0 ? level1_ : phases_[phase].levels[level];
+      if (!ncall.empty()) {
+        hl.pts.resize(tops[0]);
+        d2h(hl.pts.data(), dout_pts, sizeof(int) * tops[0], s);
+        std::vector<uint8_t> clustered(nsubs, 0);
+        std::vector<std::vector<int>> sub_calls(nsubs);
+        for (size_t j = 0; j < ncall.size(); ++j) {
+          clustered[ncall[j].sub] = 1;
+          sub_calls[ncall[j].sub].push_back((int)j);
+        }
+        std::vector<int> clist, cslot(nsubs, -1), sc_off(1, 0), sc_list;
+        for (int i = 0; i < nsubs; ++i)
+          if (clustered[i]) {
+            cslot[i] = (int)clist.size();
+            clist.push_back(i);
+            for (int j : sub_calls[i]) sc_list.push_back(j);
+            sc_off.push_back((int)sc_list.size());
+          }
+        const int ncl = (int)clist.size();
+        uint8_t* dcl = lv.get<uint8_t>(nsubs);
+        h2d(dcl, clustered.data(), nsubs, s);
+        int* dclist = lv.get<int>(ncl);
+        h2d(dclist, clist.data(), sizeof(int) * ncl, s);
+        int* dcslot = lv.get<int>(nsubs);
+        h2d(dcslot, cslot.data(), sizeof(int) * nsubs, s);
+        int* dscoff = lv.get<int>(sc_off.size());
+        h2d(dscoff, sc_off.data(), sizeof(int) * sc_off.size(), s);
+        int* dsclist = lv.get<int>(sc_list.size());
+        h2d(dsclist, sc_list.data(), sizeof(int) * sc_list.size(), s);
+        CallDesc* dncall = lv.get<CallDesc>(ncall.size());
+        h2d(dncall, ncall.data(), sizeof(CallDesc) * ncall.size(), s);
+
+        ClusterArgs CA;
+        CA.nsubs = nsubs;
+        CA.subs = dsubs;
+        CA.kstart = dkstart;
+        CA.keep_ids = keep_ids;
+        CA.keep_loff = keep_loff;
+        CA.keep_lcnt = keep_lcnt;
+        CA.lids = lids;
+        CA.bitmaps = dbm;
+        CA.words = W;
+        CA.keep_word_rank = dkwr;
+        CA.clustered = dcl;
+        CA.clustered_list = dclist;
+        CA.nkeep = K;
+        CA.n = ni;
+        CA.uf = lv.get<int>(K + 1);
+        CA.err = derr;
+        CA.guard = guard;
+        CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
+        int* is_root = lv.get<int>(K + 1);
+        int* root_id = lv.get<int>(K + 1);
+        int* comp = lv.get<int>(K + 1);
+        int* root_of = lv.get<int>(K + 1);
+        int* dsample = lv.get<int>(ncl + 1);
+        int* dnc = lv.get<int>(1);
+        long long ncomp = 0;
+        std::vector<int> cbase(nsubs + 1);
+        stats_.ms_cluster += timed(s, [&] {
+          launch_uf_init(CA.uf, K, s);
+          launch_uf_union(CA, ncl, dcslot, dsample, s);
+          launch_uf_flatten(CA, is_root, root_of, s);
+          launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
+        });
+        launches += 8;
+        ncomp = scalar(dnc, s);
+        int* dcbase = lv.get<int>(nsubs + 1);
+        launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);
+        ++launches;
+        d2h(cbase.data(), dcbase, sizeof(int) * (nsubs + 1), s);
+        int* mcount = lv.get<int>(ncomp + 1);
+        int* mfill = lv.get<int>(ncomp + 1);
+        long long* moff = lv.get<long long>(ncomp + 1);
+        int* bcount = lv.get<int>(ncomp + 1);
+        int* bfill = lv.get<int>(ncomp + 1);
+        long long* boff = lv.get<long long>(ncomp + 1);
+        CK(cudaMemsetAsync(mcount, 0, sizeof(int) * (ncomp + 1), s));
+        CK(cudaMemsetAsync(mfill, 0, sizeof(int) * (ncomp + 1), s));
+        CK(cudaMemsetAsync(bcount, 0, sizeof(int) * (ncomp + 1), s));
+        CK(cudaMemsetAsync(bfill, 0, sizeof(int) * (ncomp + 1), s));
+        long long nslots2 = (long long)ncl * n * 2;
+        int* slots = lv.get<int>(nslots2);
+        CK(cudaMemsetAsync(slots, 0xff, sizeof(int) * nslots2, s));
+        const int ovf_cap = 1 << 20;
+        int2* ovf = lv.get<int2>(ovf_cap);
+        int* novf = lv.get<int>(1);
+        CK(cudaMemsetAsync(novf, 0, sizeof(int), s));
+        long long* dmtot = lv.get<long long>(2);
+        stats_.ms_cluster += timed(s, [&] {
+          launch_comp_ids(CA, root_id, root_of, comp, mcount, s);
+          launch_exclusive_scan_i2ll(mcount, moff, ncomp, dmtot, sums, s);
+        });
+        launches += 4;
+        long long hm[2];
+        d2h(hm, dmtot, sizeof(long long), s);
+        int* members = lv.get<int>(hm[0] + 1);
+        launch_members(CA, comp, moff, mfill, members, s);
+        launches += 1;
+        int hovf = 0;
+        stats_.ms_cluster += timed(s, [&] { launch_borders(CA, comp, dcslot, slots, ovf, novf, ovf_cap, s); });
+        launches += 1;
+        hovf = scalar(novf, s);
+        if (scalar(derr, s)) throw Error(INSCY_ERR_INTERNAL, "clustering kernels reported an error");
+        check_guard("clustering");
+        hovf = std::min(hovf, ovf_cap);
+        launch_border_count(slots, nslots2, ovf, hovf, bcount, s);
+        launch_exclusive_scan_i2ll(bcount, boff, ncomp, dmtot + 1, sums, s);
+        launches += 5;
+        long long hb;
+        d2h(&hb, dmtot + 1, sizeof(long long), s);
+        int* borders = lv.get<int>(hb + 1);
+        launch_border_fill(slots, nslots2, ni, ovf, hovf, boff, bfill, borders, s);
+        // components of each region in first-seed order
+        int* firstpos = lv.get<int>(ncomp + 1);
+        CK(cudaMemsetAsync(firstpos, 0x7f, sizeof(int) * (ncomp + 1), s));
+        int* order = lv.get<int>(tops[0] + 1);
+        int* order_cnt = lv.get<int>(ncall.size());
+        stats_.ms_cluster += timed(s, [&] {
+          launch_region_order(CA, ncl, comp, dcbase, dscoff, dsclist, dncall, dout_pts, firstpos, order, order_cnt, s);
+        });
+        launches += 3;
+        // to the host
+        std::vector<long long> hmoff(ncomp + 1), hboff(ncomp + 1);
+        d2h(hmoff.data(), moff, sizeof(long long) * ncomp, s);
+        hmoff[ncomp] = hm[0];
+        d2h(hboff.data(), boff, sizeof(long long) * ncomp, s);
+        hboff[ncomp] = hb;
+        std::vector<int> hmem(hm[0]), hbor(hb);
+        d2h(hmem.data(), members, sizeof(int) * hm[0], s);
+        d2h(hbor.data(), borders, sizeof(int) * hb, s);
+        std::vector<int> hocnt(ncall.size());
+        long long* order_off = lv.get<long long>(ncall.size() + 1);
+        long long* dot = lv.get<long long>(1);
+        launch_exclusive_scan_i2ll(order_cnt, order_off, (long long)ncall.size(), dot,
+                                   scan_sums((long long)ncall.size() + 1, s, lv), s);
+        const long long norder_tot = scalar(dot, s);
+        int* packed = lv.get<int>(norder_tot + 1);
+        launch_pack_order(dncall, (int)ncall.size(), order, order_cnt, order_off, packed, s);
+        launches += 4;
+        hl.order.resize(norder_tot);
+        d2h(hl.order.data(), packed, sizeof(int) * norder_tot, s);
+        check_guard("component order");
+        d2h(hocnt.data(), order_cnt, sizeof(int) * ncall.size(), s);
+        std::vector<long long> hooff(ncall.size());
+        d2h(hooff.data(), order_off, sizeof(long long) * ncall.size(), s);
+        // one HSub per clustered subspace (component-local offsets)
+        std::vector<int> csub_of(nsubs, -1);
+        for (int i : clist) {
+          HSub hs;
+          long long c0 = cbase[i], c1 = cbase[i + 1];
+          hs.moff.resize(c1 - c0 + 1);
+          hs.boff.resize(c1 - c0 + 1);
+          for (long long c = c0; c <= c1; ++c) {
+            hs.moff[c - c0] = hmoff[c] - hmoff[c0];
+            hs.boff[c - c0] = hboff[c] - hboff[c0];
+          }
+          hs.members.assign(hmem.begin() + hmoff[c0], hmem.begin() + hmoff[c1]);
+          hs.borders.assign(hbor.begin() + hboff[c0], hbor.begin() + hboff[c1]);
+          Phase& sp = phases_[phase < 0 ? phase_of_[subs[i].dim] : phase];
+          csub_of[i] = (int)sp.subs.size();
+          sp.subs.push_back(std::move(hs));
+        }
+        for (size_t j = 0; j < ncall.size(); ++j) {
+          HCall& hc = phases_[ncall_phase[j]].calls[ncall_ids[j]];
+          hc.csub = csub_of[ncall[j].sub];
+          hc.norder = hocnt[j];
+          hc.order_off = hooff[j];
+        }
+      }
+
+      // ---- 7. advance: this level's lists become the parent lists
+      F.prev_mem.reset(keepmem.release());
+      F.prev_kstart = kstart;
+      F.keep_ids = keep_ids;
+      F.keep_loff = keep_loff;
+      F.keep_lcnt = keep_lcnt;
+      F.lids = lids;
+      F.lacc = lacc;
+      F.prev_total = L;
+      F.prev_nkeep = K;
+      F.pts_total = (long long)tops[0];
+      F.ghosts_total = (long long)tops[1];
+      F.pts_mem.reset(next_pts.release());
+      F.d_pts = dout_pts;
+      F.d_ghosts = dout_gh;
+      F.hcalls.swap(ncall);
+      F.call_ids.swap(ncall_ids);
+      lv.release();
+      stats_.kernel_launches = launches;
+      if (one_level) break;
+    }
+  };
+  expand(-1, F1, true);  // level 1: every 1-dim subspace and the root's restrictions
 
   // ---------------------------------------------------------------- commit
-  auto t_rep0 = std::chrono::steady_clock::now();
+  // A phase is committed on a second host thread as soon as its expansion is
+  // done, while this thread drives the GPU through the next phase.
   if ((int)vbuf_.size() != d + 2) vbuf_.assign(d + 2, LoopVec());
   tbits_.assign(((size_t)n + 63) / 64, 0);
   t_prune_ = t_cluster_ = t_join_ = 0;
   rc_ = stats_.replay_counters;
-  replay(0);
+  std::mutex mu;
+  std::condition_variable cv;
+  int ready = 0;
+  bool stop = false;
+  std::atomic<bool> commit_failed{false};
+  std::exception_ptr commit_err;
+  double ms_commit = 0;
+  std::thread committer([&] {
+    try {
+      for (int k = 0; k < nphases; ++k) {
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return ready > k || stop; });
+          if (stop) return;
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        for (int D = phases_[k].d0; D < phases_[k].d1; ++D) replay_root(D);
+        ms_commit += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      }
+    } catch (...) {
+      commit_err = std::current_exception();
+      commit_failed = true;
+    }
+  });
+  try {
+    for (int k = 0; k < nphases && !commit_failed; ++k) {
+      Frontier F = F1;
+      F.hcalls.clear();
+      F.call_ids.clear();
+      for (size_t i = 0; i < F1.hcalls.size(); ++i)
+        if (phase_of_[__builtin_ctzll(F1.hcalls[i].rmask)] == k) {
+          F.hcalls.push_back(F1.hcalls[i]);
+          F.call_ids.push_back(F1.call_ids[i]);
+        }
+      expand(k, F, false);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        ready = k + 1;
+      }
+      cv.notify_all();
+    }
+  } catch (...) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv.notify_all();
+    committer.join();
+    throw;
+  }
+  F1 = Frontier();
+  persist.release();
+  CK(cudaStreamSynchronize(s));
+  committer.join();
+  if (commit_err) std::rethrow_exception(commit_err);
   stats_.ms_replay_prune = t_prune_;
   stats_.ms_replay_cluster = t_cluster_;
   stats_.ms_replay_join = t_join_;
-  stats_.ms_replay = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_rep0).count();
+  stats_.ms_replay = ms_commit;
   {
     // the result map's order (vec_cmp)
     std::map<std::vector<int>, int, SubspaceOrder> order;
@@ -1235,26 +1330,52 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
 // ---------------------------------------------------------------------------
 // ordered commit (InscyNodeCpu.cu:159-235)
 // ---------------------------------------------------------------------------
-void Engine::replay(int ci) {
-  const int f = calls_[ci].f;
-  const uint64_t rmask = calls_[ci].rmask;
+// the root's loop over dim D (InscyNodeCpu.cu:171-233 at the root): every
+// region of the root on D, then join
+void Engine::replay_root(int D) {
+  const Phase& ph = phases_[phase_of_[D]];
+  LoopVec& V = vbuf_[0];
+  V.init(n_);
+  V.clear();
+  LoopState st;
+  const uint64_t smask = 1ull << D;
+  for (const HRegion& R : root_.regions) {
+    if (R.dim != D || !R.passed) continue;
+    replay(ph, R.child);
+    auto t0 = std::chrono::steady_clock::now();
+    bool ok = prune_redundancy(ph, ph.calls[R.child], smask);
+    auto t1 = std::chrono::steady_clock::now();
+    if (ok) cluster_into(ph, ph.calls[R.child], V, st);
+    auto t2 = std::chrono::steady_clock::now();
+    t_prune_ += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    t_cluster_ += std::chrono::duration<double, std::milli>(t2 - t1).count();
+  }
+  auto t3 = std::chrono::steady_clock::now();
+  join(V, st, smask);
+  t_join_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t3).count();
+}
+
+void Engine::replay(const Phase& ph, int ci) {
+  const HCall& c = ph.calls[ci];
+  const int f = c.f;
+  const uint64_t rmask = c.rmask;
   const int depth = __builtin_popcountll(rmask);
   LoopVec& V = vbuf_[depth];
   V.init(n_);
   size_t ri = 0;
-  const size_t nreg = calls_[ci].regions.size();
+  const size_t nreg = c.regions.size();
   for (int D = f; D < d_; ++D) {
     const uint64_t smask = rmask | (1ull << D);
     LoopState st;
     V.clear();
-    while (ri < nreg && calls_[ci].regions[ri].dim == D) {
-      const HRegion R = calls_[ci].regions[ri++];
+    while (ri < nreg && c.regions[ri].dim == D) {
+      const HRegion R = c.regions[ri++];
       if (!R.passed) continue;
-      replay(R.child);
+      replay(ph, R.child);
       auto t0 = std::chrono::steady_clock::now();
-      bool ok = prune_redundancy(calls_[R.child], smask);
+      bool ok = prune_redundancy(ph, ph.calls[R.child], smask);
       auto t1 = std::chrono::steady_clock::now();
-      if (ok) cluster_into(calls_[R.child], V, st);
+      if (ok) cluster_into(ph, ph.calls[R.child], V, st);
       auto t2 = std::chrono::steady_clock::now();
       t_prune_ += std::chrono::duration<double, std::milli>(t1 - t0).count();
       t_cluster_ += std::chrono::duration<double, std::milli>(t2 - t1).count();
@@ -1297,8 +1418,8 @@ static void refresh_order(Entry& E) {
   E.dirty = false;
 }
 
-bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
-  const int* pts = levels_[c.level].pts.data() + c.pts_off;
+bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
+  const int* pts = level_of(ph, c).pts.data() + c.pts_off;
   const int m = c.npts;
   rc_[6]++;
   const double thr = (double)((float)m * hp_.r);
@@ -1326,7 +1447,7 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
       refresh_order(E);
       for (int l : E.by_size) {
         bool hit = false;
-        const HSub& hs = subs_[E.src[l].csub];
+        const HSub& hs = *E.src[l].hs;
         const int cp = E.src[l].comp;
         for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
           int q = hs.members[k];
@@ -1357,9 +1478,9 @@ bool Engine::prune_redundancy(const HCall& c, uint64_t smask) {
 // BFS numbering of INSCYClusteringImplCPUAll (ClusteringCpu.cu:317-389):
 // components in the order their first dense seed appears, members get the
 // next label, non-dense neighbours that are still -1 become -2.
-void Engine::cluster_into(const HCall& c, LoopVec& V, LoopState& st) {
-  const HSub& hs = subs_[c.csub];
-  const int* order = levels_[c.level].order.data() + c.order_off;
+void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState& st) {
+  const HSub& hs = ph.subs[c.csub];
+  const int* order = level_of(ph, c).order.data() + c.order_off;
   // labels in first-seed order.  Components are disjoint and their border
   // points are not dense, so no write below changes another component's
   // first member: all labels can be decided before the writes.
@@ -1373,7 +1494,7 @@ void Engine::cluster_into(const HCall& c, LoopVec& V, LoopState& st) {
     ++st.nlabels;
     rc_[8]++;
     rc_[9] += hs.boff[comp + 1] - hs.boff[comp];
-    st.ref.push_back(LabelRef{c.csub, comp});
+    st.ref.push_back(LabelRef{&hs, comp});
     st.size.push_back((int)(m1 - m0));
     work += (m1 - m0) + (hs.boff[comp + 1] - hs.boff[comp]);
   }
@@ -1456,7 +1577,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         const int l = H.by_size[t];
         const int hsz = H.size[l];
         if (!((float)minsz * hp_.r < (float)hsz)) break;
-        const HSub& hs = subs_[H.src[l].csub];
+        const HSub& hs = *H.src[l].hs;
         const int cp = H.src[l].comp;
         const long long m = hs.moff[cp + 1] - hs.moff[cp];
         walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, m, H.lab.data(), l, (float)hsz});
@@ -1501,7 +1622,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       bool hit = false;
       for (int l = 1; l <= nl; ++l) {
         if (!alive[l]) continue;
-        const HSub& hs = subs_[st.ref[l].csub];
+        const HSub& hs = *st.ref[l].hs;
         const int cp = st.ref[l].comp;
         for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
           const int q = hs.members[k];
@@ -1547,7 +1668,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   const int top = off + nl;
   if ((int)E->size.size() <= top) {
     E->size.resize(top + 1, 0);
-    E->src.resize(top + 1, LabelRef{-1, -1});
+    E->src.resize(top + 1, LabelRef{nullptr, -1});
   }
   // label sizes and sources, then the point writes: members of the live
   // clusters get their new label, border marks of every cluster overwrite
@@ -1555,7 +1676,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   pieces_.clear();
   long long work = 0;
   for (int l = 1; l <= nl; ++l) {
-    const HSub& hs = subs_[st.ref[l].csub];
+    const HSub& hs = *st.ref[l].hs;
     const int cp = st.ref[l].comp;
     if (alive[l]) {
       const int nv = off + l;
