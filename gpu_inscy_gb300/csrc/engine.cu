@@ -918,6 +918,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       // ---- 4. restrict / merge / prune of every (call, dim)
       const int ncalls = (int)F.hcalls.size();
       std::vector<long long> work_off(ncalls), work_scr;
+      std::vector<int> items_big, items_small;  // work items by block size (see launch_tree_level)
       long long nwork = 0, scr = 0, pts_cap = 0, ghost_in = 0;
       for (int i = 0; i < ncalls; ++i) {
         work_off[i] = nwork;
@@ -929,11 +930,20 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
                             4LL * (3LL * F.hcalls[i].npts + 1 + 2LL * F.hcalls[i].nghost);
           scr += (bytes + 15) / 16 * 16;
         }
+        for (int t = 0; t < nd; ++t)
+          ((long long)F.hcalls[i].npts + F.hcalls[i].nghost > kTreeBig ? items_big : items_small)
+              .push_back((int)(nwork + t));
         nwork += nd;
         pts_cap += (long long)F.hcalls[i].npts * nd;
         ghost_in += (long long)F.hcalls[i].nghost * nd;
       }
-      stats_.regions += 0;
+      int* ditems = nullptr;
+      if (!items_big.empty()) {
+        std::vector<int> both(items_big);
+        both.insert(both.end(), items_small.begin(), items_small.end());
+        ditems = lv.get<int>(both.size());
+        h2d(ditems, both.data(), sizeof(int) * both.size(), s);
+      }
       CallDesc* dcalls = lv.get<CallDesc>(ncalls);
       h2d(dcalls, F.hcalls.data(), sizeof(CallDesc) * ncalls, s);
       long long* dwork = lv.get<long long>(ncalls);
@@ -986,8 +996,12 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         TL.pts_in_total = F.pts_total;
         TL.ghosts_in_total = F.ghosts_total;
         TL.guard = guard;
+        TL.items_big = ditems;
+        TL.nbig = ditems ? (int)items_big.size() : 0;
+        TL.items_small = ditems ? ditems + items_big.size() : nullptr;
+        TL.nsmall = ditems ? (int)items_small.size() : 0;
         stats_.ms_tree += timed(s, [&] { launch_tree_level(TL, s); });
-        ++launches;
+        launches += (TL.nbig > 0 && TL.nsmall > 0) ? 2 : 1;
         int err = scalar(derr, s);
         d2h(tops, dtops, sizeof(tops), s);
         if (err == 2 && attempt < 4) {

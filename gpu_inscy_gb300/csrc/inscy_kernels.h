@@ -105,7 +105,18 @@ struct TreeLaunch {
   long long pts_in_total;
   long long ghosts_in_total;
   Guard guard;
+  // work items with more than kTreeBig points + chains (nbig of them, listed
+  // in items_big) run in 1024-thread blocks, the others (items_small) in
+  // 256-thread blocks; nbig = 0: every item in one 256-thread launch
+  const int* items_big;
+  int nbig;
+  const int* items_small;
+  int nsmall;
 };
+#ifndef INSCY_TREE_BIG
+#define INSCY_TREE_BIG 4096
+#endif
+constexpr long long kTreeBig = INSCY_TREE_BIG;
 void launch_tree_level(const TreeLaunch& L, cudaStream_t s);
 
 // ---- clustering (kernels_cluster.cu)

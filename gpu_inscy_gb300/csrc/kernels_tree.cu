@@ -38,8 +38,12 @@
 
 namespace inscy {
 
+// Work items (one call, one dim) of up to kTreeBig points and chains get a
+// block of 256 threads; larger ones a block of 1024 in a separate launch, so a
+// level's few large items (the root's restrictions hold every point) do not
+// leave the GPU waiting on a long tail.
 constexpr int kTreeThreads = 256;
-constexpr int kTreeWarps = kTreeThreads / 32;
+constexpr int kTreeThreadsBig = 1024;
 
 using Key = unsigned __int128;
 
@@ -90,6 +94,7 @@ __device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) 
 
 // one stable counting-sort pass of (key, value) pairs by an 8-bit digit of
 // the key (warp match for the intra-warp rank, block scan across warps)
+template <int kWarps>
 __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* vout, int n, int shift, int* s_base,
                                 int* s_tot, int* s_wc) {
   const int R = 256;
@@ -118,7 +123,7 @@ __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* 
   }
   __syncthreads();
   for (int c0 = 0; c0 < n; c0 += blockDim.x) {
-    for (int i = threadIdx.x; i < kTreeWarps * R; i += blockDim.x) s_wc[i] = 0;
+    for (int i = threadIdx.x; i < kWarps * R; i += blockDim.x) s_wc[i] = 0;
     __syncthreads();
     int j = c0 + threadIdx.x;
     bool valid = j < n;
@@ -131,7 +136,7 @@ __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* 
     __syncthreads();
     for (int u = threadIdx.x; u < R; u += blockDim.x) {
       int run = 0;
-      for (int w = 0; w < kTreeWarps; ++w) {
+      for (int w = 0; w < kWarps; ++w) {
         int t = s_wc[w * R + u];
         s_wc[w * R + u] = run;
         run += t;
@@ -150,6 +155,7 @@ __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* 
   }
 }
 
+template <int kWarps>
 struct TreeShared {
   int cnt[256];
   int sf[256];
@@ -160,7 +166,7 @@ struct TreeShared {
   int sh[32];
   int base[256];
   int tot[256];
-  int wc[kTreeWarps * 256];
+  int wc[kWarps * 256];
   long long off;
   long long goff;
   int gcount;
@@ -199,10 +205,13 @@ __device__ __forceinline__ void key_range(const Key* K, int m, Key key, int sh, 
   hi = a;
 }
 
-__global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
-  __shared__ TreeShared s;
-  const int w = blockIdx.x;
-  if (w >= a.nwork) return;
+// one block per work item: items[blockIdx.x], or blockIdx.x without a list
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* __restrict__ items, int nitems) {
+  __shared__ TreeShared<kThreads / 32> s;
+  if ((int)blockIdx.x >= nitems) return;
+  const int w = items ? items[blockIdx.x] : (int)blockIdx.x;
+  if (w < 0 || w >= a.nwork) return;
   // locate the call of this work item
   int lo = 0, hi = a.ncalls - 1;
   while (lo < hi) {
@@ -316,7 +325,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
       Key* koth = KB;
       int* oth = B;
       for (int sh = 0; sh < key_bits; sh += 8) {
-        block_sort_pass(kcur, cur, koth, oth, m, sh, s.base, s.tot, s.wc);
+        block_sort_pass<kThreads / 32>(kcur, cur, koth, oth, m, sh, s.base, s.tot, s.wc);
         Key* tk = kcur;
         kcur = koth;
         koth = tk;
@@ -390,7 +399,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_level(TreeArgs a) {
           int* gc = GA;
           int* go = GB;
           for (int sh = 0; sh < key_bits; sh += 8) {
-            block_sort_pass(kc, gc, ko, go, ngp, sh, s.base, s.tot, s.wc);
+            block_sort_pass<kThreads / 32>(kc, gc, ko, go, ngp, sh, s.base, s.tot, s.wc);
             Key* tk = kc;
             kc = ko;
             ko = tk;
@@ -545,7 +554,12 @@ void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
   a.pts_in_total = L.pts_in_total;
   a.ghosts_in_total = L.ghosts_in_total;
   a.guard = L.guard;
-  k_tree_level<<<L.nwork, kTreeThreads, 0, s>>>(a);
+  if (L.nbig > 0) {
+    k_tree_level<kTreeThreadsBig><<<L.nbig, kTreeThreadsBig, 0, s>>>(a, L.items_big, L.nbig);
+    if (L.nsmall > 0) k_tree_level<kTreeThreads><<<L.nsmall, kTreeThreads, 0, s>>>(a, L.items_small, L.nsmall);
+  } else {
+    k_tree_level<kTreeThreads><<<L.nwork, kTreeThreads, 0, s>>>(a, nullptr, L.nwork);
+  }
 }
 
 }  // namespace inscy

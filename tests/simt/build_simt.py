@@ -4,7 +4,8 @@ The kernel launches `k<<<grid, block, smem, stream>>>(args)` of the engine's
 .cu files are rewritten into `simt::launch("k", grid, block, [=] { k(args); })`
 and the files compiled as C++ against tests/simt/cuda_runtime.h.  The device
 self-test file that names a device symbol is left out (the harness has no
-device symbols).  Output: gpu_inscy_gb300/_build/simt/driver.
+device symbols).  Output: gpu_inscy_gb300/_build/simt<tag>/driver; `defines`
+set the engine's build-time tunables.
 """
 import os
 import shutil
@@ -74,8 +75,9 @@ def rewrite_launches(text):
         i = q + 1
 
 
-def build(verbose=False):
-    src = os.path.join(OUT, "src")
+def build(verbose=False, defines=(), tag=""):
+    out = OUT + tag
+    src = os.path.join(out, "src")
     if os.path.isdir(src):
         shutil.rmtree(src)
     os.makedirs(src)
@@ -95,10 +97,10 @@ def build(verbose=False):
     # no _FORTIFY_SOURCE: its longjmp check rejects the jumps between fiber stacks
     flags = ["g++", "-std=c++17", "-O2", "-g", "-U_FORTIFY_SOURCE", "-D_FORTIFY_SOURCE=0", "-ffp-contract=off",
              "-fno-strict-aliasing", "-w",
-             "-I" + HERE, "-I" + os.path.join(ROOT, "include"), "-I" + src]
+             "-I" + HERE, "-I" + os.path.join(ROOT, "include"), "-I" + src] + ["-D" + x for x in defines]
 
     def cc(u):
-        obj = os.path.join(OUT, os.path.basename(u) + ".o")
+        obj = os.path.join(out, os.path.basename(u) + ".o")
         r = subprocess.run(flags + ["-c", u, "-o", obj], capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError("compiling %s:\n%s" % (u, r.stderr[-4000:]))
@@ -106,7 +108,7 @@ def build(verbose=False):
 
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         objs = list(ex.map(cc, units))
-    exe = os.path.join(OUT, "driver")
+    exe = os.path.join(out, "driver")
     subprocess.run(["g++", "-o", exe] + objs + ["-lpthread"], check=True)
     if verbose:
         print(exe)

@@ -70,6 +70,13 @@ def test_family_cases(driver):
 
 
 @pytest.fixture(scope="module")
+def driver_big_blocks():
+    # every level-kernel work item above 64 points takes the 1024-thread path
+    import build_simt
+    return build_simt.build(defines=("INSCY_TREE_BIG=64",), tag="_treebig")
+
+
+@pytest.fixture(scope="module")
 def plain_case():
     # the 25,000 x 15 workload's generator and parameters at a size the oracle finishes fast
     X = synth.make_plain(3, n=1000)
@@ -81,3 +88,11 @@ def plain_case():
 def test_plain_workload_shape(driver, plain_case, reverse):
     X, p, want = plain_case
     assert_same(simt_run(driver, X, p, reverse, "plain"), want, "plain n=1000")
+
+
+@pytest.mark.parametrize("reverse", [False, True], ids=["warps-up", "warps-down"])
+def test_level_kernel_large_blocks(driver_big_blocks, plain_case, reverse):
+    X, p, want = plain_case
+    assert_same(simt_run(driver_big_blocks, X, p, reverse, "plain_big"), want, "plain n=1000, 1024-thread items")
+    X, p, want = small_case(0)
+    assert_same(simt_run(driver_big_blocks, X, p, reverse, "small_big"), want, "small, 1024-thread items")
