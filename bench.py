@@ -242,7 +242,8 @@ def main():
             "roofline": roof, "clocks": clk,
             "breakdown_ms": {k: st[k] for k in ("ms_setup", "ms_density", "ms_density_pass1", "ms_tree",
                                                "ms_cluster", "ms_replay", "ms_replay_prune", "ms_replay_cluster",
-                                               "ms_replay_join", "ms_d2h", "ms_total")},
+                                               "ms_replay_join", "ms_d2h", "ms_expand", "ms_commit_tail",
+                                               "ms_total")},
             "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
             "commit_counters": st["replay"],
             "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}

@@ -38,7 +38,8 @@ class Stats(ctypes.Structure):
                  "ms_replay_prune", "ms_replay_cluster", "ms_replay_join", "ms_d2h", "density_bytes", "tree_bytes")] + \
                [(name, ctypes.c_longlong) for name in
                 ("density_launches_pass1", "kernel_launches", "calls", "regions", "subspaces", "candidates",
-                 "levels", "h2d_bytes", "d2h_bytes")] + [("replay_counters", ctypes.c_longlong * 10)]
+                 "levels", "h2d_bytes", "d2h_bytes")] + [("replay_counters", ctypes.c_longlong * 10), ("ms_expand", ctypes.c_double),
+                                               ("ms_commit_tail", ctypes.c_double)]
 
     COUNTERS = ("joins", "new_entries", "label_writes", "border_writes", "superset_entries", "redundancy_points",
                 "prune_calls", "prune_points", "clusters_numbered", "border_checks")

@@ -1318,7 +1318,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   F1 = Frontier();
   persist.release();
   CK(cudaStreamSynchronize(s));
+  auto t_expanded = std::chrono::steady_clock::now();
+  stats_.ms_expand = std::chrono::duration<double, std::milli>(t_expanded - t_start).count();
   committer.join();
+  stats_.ms_commit_tail = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_expanded).count();
   if (commit_err) std::rethrow_exception(commit_err);
   stats_.ms_replay_prune = t_prune_;
   stats_.ms_replay_cluster = t_cluster_;

@@ -83,6 +83,8 @@ typedef struct inscy_stats {
    * join's redundancy test, pruneRedundancy calls, points visited by
    * pruneRedundancy, clusters numbered, border checks while numbering */
   long long replay_counters[10];
+  double ms_expand;       /* wall time of the expansion (the GPU-driving thread) */
+  double ms_commit_tail;  /* time the run waited for the commit once the expansion was done */
 } inscy_stats;
 
 /* Replaces run_gpu_5 / run_gpu_4 (inscy_map.cpp:1070-1158 / :979-1067).
