@@ -257,10 +257,13 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
 
 // density of every (subspace, point) from its list.  The phi sum of one item
 // is sequential, so each lane walks its own list; lists differ a lot in
-// length, so every warp owns kFlagsItems consecutive items as a queue: a lane
+// length, so every warp owns `per_warp` consecutive items as a queue: a lane
 // that finishes an item takes the next one, and all busy lanes advance
-// together for as many entries as the shortest remaining list allows.
-constexpr int kFlagsItems = 256;
+// together for as many entries as the shortest remaining list allows.  The
+// queue length is chosen so that the level still fills the GPU with warps
+// (32 items, one per lane, when there are few; up to 256).
+constexpr int kFlagsMaxItems = 256;
+constexpr long long kFlagsWarpsWanted = 152LL * 48;  // SMs x resident warps to aim for
 
 __device__ __forceinline__ void flags_finish(const DensityArgs& a, long long item, float v) {
   const int si = find_sub(a.subs, a.nsubs, item);
@@ -279,10 +282,10 @@ __device__ __forceinline__ void flags_finish(const DensityArgs& a, long long ite
   if (f & kFlagKeep) atomicOr(bm + 2 * a.words, bit);
 }
 
-__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a) {
-  const long long first = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kFlagsItems;
+__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a, int per_warp) {
+  const long long first = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * per_warp;
   if (first >= a.nitems) return;  // whole warps
-  const long long last = first + kFlagsItems < a.nitems ? first + kFlagsItems : a.nitems;
+  const long long last = first + per_warp < a.nitems ? first + per_warp : a.nitems;
   const unsigned lane = lane_id();
   long long next = first + 32;  // next item of the queue (the same in every lane)
   long long item = first + lane;
@@ -507,8 +510,10 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s) {
   if (L.nitems <= 0) return;
   DensityArgs a = make_args(L);
-  const long long warps = (L.nitems + kFlagsItems - 1) / kFlagsItems;
-  k_density_flags<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(a);
+  long long per_warp = (L.nitems / kFlagsWarpsWanted + 31) / 32 * 32;
+  per_warp = per_warp < 32 ? 32 : per_warp > kFlagsMaxItems ? kFlagsMaxItems : per_warp;
+  const long long warps = (L.nitems + per_warp - 1) / per_warp;
+  k_density_flags<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(a, (int)per_warp);
 }
 
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,

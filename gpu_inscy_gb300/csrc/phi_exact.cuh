@@ -1,5 +1,7 @@
 // The reference's phi step, sum = float(double(sum) + (1.0 - double(sq)))
-// (ClusteringCpu.cu:118-120), computed exactly with 64-bit integer arithmetic.
+// (ClusteringCpu.cu:118-120), computed exactly with integer arithmetic:
+// phi_step_exact (32-bit integers, the common case) and phi_step_u64 (64-bit,
+// every sum; the derivation below).
 //
 // GB300's FP64 rate is a small fraction of its FP32/INT32 rate, and this step
 // runs once per (neighbour, subspace, point).  In units of 2^-53:
@@ -65,7 +67,8 @@ PHI_HD float phi_step_double(float sum, float sq) {
   return (float)((double)sum + (1.0 - (double)sq));
 }
 
-PHI_HD float phi_step_exact(float sum, float sq) {
+// the general form on 64-bit integers
+PHI_HD float phi_step_u64(float sum, float sq) {
   const uint32_t sb = f2u(sum), qb = f2u(sq);
   const uint32_t bs = sb >> 23, bq = qb >> 23;
   if ((sb != 0 && (bs < 127 - 24 || bs > 254)) || qb > 0x3f800000u) return phi_step_double(sum, sq);
@@ -110,6 +113,74 @@ PHI_HD float phi_step_exact(float sum, float sq) {
     ++e;
   }
   return u2f(((uint32_t)(e + 127) << 23) | ((uint32_t)q & 0x7fffffu));
+}
+
+
+PHI_HD float sub_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+
+// The common case on 32-bit integers (64-bit shifts occupy a slow pipe on
+// GB300): 1 <= sum < 2^24 and sq in {0} u [2^-30, 1].  Units of
+// q = 2^(e - 24), e the exponent of sum: sum = S (in [2^24, 2^25)), 1 = 2^(24-e),
+// sq = I + F (integer part, fraction F = Fsq / 2^fb) and V = sum + 1 - sq <
+// 2^26.  The double addition rounds V to 28 fraction bits (27 once V >= 2^25,
+// i.e. past the next power of two), half to even; the conversion to float
+// then rounds to a multiple of 2 (4) units -- both shifts together are 29
+// bits, so the second rounding is a remainder test against 2^28.
+// sum = 0 is one correctly rounded subtraction; the rest takes phi_step_u64.
+PHI_HD float phi_step_exact(float sum, float sq) {
+  const uint32_t sb = f2u(sum), qb = f2u(sq);
+  const uint32_t bs = sb >> 23, bq = qb >> 23;
+  const bool q_ok = qb == 0 || (bq >= 127 - 30 && qb <= 0x3f800000u);
+  if (sb == 0 && q_ok) return sub_rn(1.f, sq);  // 1 - sq is exact in double here
+  if (!q_ok || bs < 127 || bs > 127 + 23) return phi_step_u64(sum, sq);
+  const int e = (int)bs - 127;
+  const uint32_t S = ((sb & 0x7fffffu) | 0x800000u) << 1;
+  const uint32_t one = 1u << (24 - e);
+  uint32_t I = 0, Fsq = 0;
+  int fb = 0;
+  if (qb != 0) {
+    const uint32_t mq = (qb & 0x7fffffu) | 0x800000u;
+    const int k1 = (int)bq - 127 - e + 1;  // sq = mq * 2^k1 units, k1 <= 1
+    if (k1 >= 0) {
+      I = mq << k1;
+    } else {
+      fb = -k1;
+      I = fb >= 24 ? 0u : mq >> fb;
+      Fsq = fb >= 24 ? mq : mq & ((1u << fb) - 1u);
+    }
+  }
+  const uint32_t Vi = S + one - I;  // V = Vi - Fsq / 2^fb
+  const int up = (Vi - (Fsq != 0 ? 1u : 0u)) >= (1u << 25) ? 1 : 0;
+  const int fr = 28 - up;
+  uint32_t RF;  // the fraction on the double's grid: Fsq * 2^(fr - fb), half to even
+  if (fb <= fr) {
+    RF = Fsq << (fr - fb);
+  } else {
+    const int r = fb - fr;  // 1 .. 25; Fsq < 2^24
+    const uint32_t qv = Fsq >> r, rem = Fsq & ((1u << r) - 1u), half = 1u << (r - 1);
+    RF = qv + ((rem > half || (rem == half && (qv & 1u))) ? 1u : 0u);
+  }
+  // round (Vi * 2^fr - RF) / 2^29 half to even
+  const int g = 1 + up;  // float grid of the result: 2^g units
+  uint32_t Q = Vi >> g;
+  int32_t rem = (int32_t)((Vi & ((1u << g) - 1u)) << fr) - (int32_t)RF;
+  if (rem < 0) {
+    Q -= 1;
+    rem += 1 << 29;
+  }
+  Q += (rem > (1 << 28) || (rem == (1 << 28) && (Q & 1u))) ? 1u : 0u;
+  int ex = e + up;
+  if (Q >> 24) {
+    Q >>= 1;
+    ++ex;
+  }
+  return u2f(((uint32_t)(ex + 127) << 23) | (Q & 0x7fffffu));
 }
 
 }  // namespace inscy

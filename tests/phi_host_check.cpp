@@ -35,12 +35,18 @@ int main(int argc, char** argv) {
   for (long long i = 0; i < n; ++i) {
     const uint64_t x = mix((uint64_t)i * 0x9e3779b97f4a7c15ull + 1), y = mix(x + 0x632be59bd9b4e019ull);
     float sum;
-    switch (x & 3) {
+    switch (x & 7) {
       case 0:  // an integer-valued count
         sum = (float)((x >> 8) % 3000);
         break;
-      case 1:  // the range phi sums take
+      case 1:
+      case 2:  // the range phi sums take
         sum = u2f((uint32_t)(((x >> 8) % 34 + 127 - 24) << 23) | (uint32_t)((x >> 20) & 0x7fffffu));
+        break;
+      case 3:
+      case 4:
+      case 5:  // [1, 2^13): most steps of the density kernel
+        sum = u2f((uint32_t)(((x >> 8) % 13 + 127) << 23) | (uint32_t)((x >> 20) & 0x7fffffu));
         break;
       default:  // wide exponents
         sum = u2f((uint32_t)(((x >> 8) % 90 + 127 - 30) << 23) | (uint32_t)((x >> 20) & 0x7fffffu));
