@@ -65,6 +65,11 @@ struct Error : std::runtime_error {
 // types (ClusteringCpu.cu:27, 36-38, 136-164)
 // ---------------------------------------------------------------------------
 const double kPi = 3.14;  // ClusteringCpu.cu:27
+// device memory the single-pass neighbour lists of one level may take
+#ifndef INSCY_SINGLE_PASS_BYTES
+#define INSCY_SINGLE_PASS_BYTES (32LL << 30)
+#endif
+constexpr long long kSinglePassBytes = INSCY_SINGLE_PASS_BYTES;
 static float omega_of(int k) { return (float)(2.0 / ((double)k + 2.0)); }
 static float gamma_of(int m) {
   if (m == 2) return 1.0f;
@@ -835,54 +840,101 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.prev_nkeep = F.prev_nkeep;
       DL.total = 0;
       DL.guard = guard;
-      unsigned long long* dcand_cnt = lv.get<unsigned long long>(2);
-      CK(cudaMemsetAsync(dcand_cnt, 0, 2 * sizeof(unsigned long long), s));
+      unsigned long long* dcand_cnt = lv.get<unsigned long long>(3);
+      CK(cudaMemsetAsync(dcand_cnt, 0, 3 * sizeof(unsigned long long), s));
       DL.cand_counter = dcand_cnt;
       DL.list_counter = dcand_cnt + 1;
+      DL.out_counter = dcand_cnt + 2;
+      DL.cap_base = nullptr;
+      DL.cap_loff = nullptr;
       auto neighbours = [&](bool write) {
         if (level == 1)
           launch_neighbours(DL, write, s);
         else
           launch_neighbours_multi(DL, ngroup_warps, write, s);
       };
-      double ms1 = timed(s, [&] { neighbours(false); });
-      stats_.ms_density += ms1;
-      stats_.ms_density_pass1 += ms1;
-      stats_.density_launches_pass1 += 1;
-      ++launches;
-      {
-        // algorithmic bytes of the count pass: per (subspace, point) 26 B (its
-        // id, list offset and length, own coordinate and fine cell, count out);
-        // per list entry read 8 B (id + partial distance; at level 1 id +
-        // coordinate); per further (candidate, child subspace) test at levels
-        // >= 2 5 B (the candidate's coordinate and fine cell on that dim)
-        unsigned long long nc[2];
+      // algorithmic bytes of the candidate pass: per (subspace, point) 26 B (its
+      // id, list offset and length, own coordinate and fine cell, count out);
+      // per list entry read 8 B (id + partial distance; at level 1 id +
+      // coordinate); per further (candidate, child subspace) test at levels
+      // >= 2 5 B (the candidate's coordinate and fine cell on that dim); per
+      // entry written by the single pass 8 B
+      auto count_bytes = [&](bool single) {
+        unsigned long long nc[3];
         d2h(nc, dcand_cnt, sizeof(nc), s);
         stats_.candidates += (long long)nc[0];
-        stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] + (level == 1 ? 0.0 : 5.0 * (double)nc[0]);
-      }
-      check_guard("density count");  // the counts size every later buffer
-      DL.cand_counter = nullptr;
-      DL.list_counter = nullptr;
+        stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] +
+                                (level == 1 ? 0.0 : 5.0 * (double)nc[0]) + (single ? 8.0 * (double)nc[2] : 0.0);
+      };
 
-      // ---- 3. ordered lists of every item, then densities and flags
+      // ---- 3. ordered lists of every item, then densities and flags.  At
+      // levels >= 2 a child's list is a subsequence of the parent's, so when
+      // the parent lengths bound the level within kSinglePassBytes one pass
+      // tests and writes (lists at capacity offsets); otherwise a count pass
+      // sizes the lists exactly and a second pass writes them.
       long long* dloff = lv.get<long long>(nitems);
       long long* dtot = lv.get<long long>(2);
-      void* sums = scan_sums(std::max(nitems, (long long)nsubs * W) + 1, s, lv);
-      launch_exclusive_scan_i2ll(dcnt, dloff, nitems, dtot, sums, s);
-      launches += 3;
-      const long long L = scalar(dtot, s);
-      int* lids = keepmem->get<int>(L);
-      float* lacc = keepmem->get<float>(L);
-      DL.loff = dloff;
-      DL.lids = lids;
-      DL.lacc = lacc;
-      DL.total = L;
-      stats_.ms_density += timed(s, [&] {
-        neighbours(true);
-        launch_density_flags(DL, s);
-      });
-      launches += 2;
+      void* sums = scan_sums(std::max(std::max(nitems, (long long)nsubs * W), ngroup_warps) + 1, s, lv);
+      long long L = 0;
+      int* lids = nullptr;
+      float* lacc = nullptr;
+      bool single = false;
+      if (level > 1) {
+        long long* cap = lv.get<long long>(ngroup_warps + 1);
+        long long* cbase = lv.get<long long>(ngroup_warps + 1);
+        launch_list_capacity(DL, ngroup_warps, cap, s);
+        launch_exclusive_scan_ll(cap, cbase, ngroup_warps, dtot, sums, s);
+        launches += 4;
+        const long long capt = scalar(dtot, s);
+        if (capt * 8 <= kSinglePassBytes) {
+          single = true;
+          L = capt;
+          lids = keepmem->get<int>(L);
+          lacc = keepmem->get<float>(L);
+          DL.cap_base = cbase;
+          DL.cap_loff = dloff;
+          DL.lids = lids;
+          DL.lacc = lacc;
+          DL.total = L;
+          const double ms1 = timed(s, [&] { neighbours(true); });
+          stats_.ms_density += ms1;
+          stats_.ms_density_pass1 += ms1;
+          stats_.density_launches_pass1 += 1;
+          ++launches;
+          count_bytes(true);
+          check_guard("density lists");
+          DL.cap_base = nullptr;
+          DL.cap_loff = nullptr;
+          DL.cand_counter = DL.list_counter = DL.out_counter = nullptr;
+          DL.loff = dloff;
+          stats_.ms_density += timed(s, [&] { launch_density_flags(DL, s); });
+          ++launches;
+        }
+      }
+      if (!single) {
+        const double ms1 = timed(s, [&] { neighbours(false); });
+        stats_.ms_density += ms1;
+        stats_.ms_density_pass1 += ms1;
+        stats_.density_launches_pass1 += 1;
+        ++launches;
+        count_bytes(false);
+        check_guard("density count");  // the counts size every later buffer
+        DL.cand_counter = DL.list_counter = DL.out_counter = nullptr;
+        launch_exclusive_scan_i2ll(dcnt, dloff, nitems, dtot, sums, s);
+        launches += 3;
+        L = scalar(dtot, s);
+        lids = keepmem->get<int>(L);
+        lacc = keepmem->get<float>(L);
+        DL.loff = dloff;
+        DL.lids = lids;
+        DL.lacc = lacc;
+        DL.total = L;
+        stats_.ms_density += timed(s, [&] {
+          neighbours(true);
+          launch_density_flags(DL, s);
+        });
+        launches += 2;
+      }
       // kept items
       int* dkcnt = lv.get<int>(nitems);
       int* dkflag = lv.get<int>(nitems);

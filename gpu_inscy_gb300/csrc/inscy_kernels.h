@@ -56,6 +56,9 @@ struct DensityLaunch {
   float* lacc;
   unsigned long long* cand_counter;
   unsigned long long* list_counter;
+  unsigned long long* out_counter;  // single-pass write: entries written
+  const long long* cap_base;        // single-pass write: list base of every (group, query)
+  long long* cap_loff;              // single-pass write: list start of every item (out)
   long long prev_total;
   long long total;
   long long prev_nkeep;
@@ -63,6 +66,7 @@ struct DensityLaunch {
 };
 void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s);
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s);
+void launch_list_capacity(const DensityLaunch& L, long long nwarps, long long* cap, cudaStream_t s);
 void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
 void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s);
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,

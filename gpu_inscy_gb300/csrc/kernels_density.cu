@@ -63,6 +63,12 @@ struct DensityArgs {
   float* lacc;
   unsigned long long* cand_counter;  // candidate tests (candidate x child subspace)
   unsigned long long* list_counter;  // list entries read
+  unsigned long long* out_counter;   // list entries written (single-pass write)
+  // single-pass write (levels >= 2): the list of child c of (group, query) w
+  // starts at cap_base[w] + c * (the query's parent-list length), a bound on
+  // its length; the kernel writes every item's count and list start (cap_loff)
+  const long long* cap_base;
+  long long* cap_loff;
   long long prev_total;  // entries in the previous level's lists
   long long total;       // entries in this level's lists (write passes)
   long long prev_nkeep;  // kept points of the previous level
@@ -201,7 +207,11 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
   const uint8_t* frow_p = a.fc + (size_t)p * a.d;
   int run0 = 0, run1 = 0;  // lane c: children c and c + 32
   long long ob0 = 0, ob1 = 0;
-  if (kWrite) {
+  const bool single = kWrite && a.cap_base != nullptr;
+  if (single) {
+    ob0 = a.cap_base[w] + (long long)lane * len;
+    ob1 = a.cap_base[w] + (long long)(lane + 32) * len;
+  } else if (kWrite) {
     if ((int)lane < nc) ob0 = a.loff[a.subs[g.sub_base + lane].item_off + i];
     if ((int)lane + 32 < nc) ob1 = a.loff[a.subs[g.sub_base + lane + 32].item_off + i];
   }
@@ -247,12 +257,46 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
       }
     }
   }
-  if (!kWrite) {
-    if ((int)lane < nc) a.cnt[a.subs[g.sub_base + lane].item_off + i] = run0;
-    if ((int)lane + 32 < nc) a.cnt[a.subs[g.sub_base + lane + 32].item_off + i] = run1;
+  if (!kWrite || single) {
+    if ((int)lane < nc) {
+      const long long item = a.subs[g.sub_base + lane].item_off + i;
+      a.cnt[item] = run0;
+      if (single) a.cap_loff[item] = ob0;
+    }
+    if ((int)lane + 32 < nc) {
+      const long long item = a.subs[g.sub_base + lane + 32].item_off + i;
+      a.cnt[item] = run1;
+      if (single) a.cap_loff[item] = ob1;
+    }
     if (lane == 0 && a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len * nc);
     if (lane == 0 && a.list_counter) atomicAdd(a.list_counter, (unsigned long long)len);
+    if (single && a.out_counter) {
+      int tot = ((int)lane < nc ? run0 : 0) + ((int)lane + 32 < nc ? run1 : 0);
+      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+      if (lane == 0) atomicAdd(a.out_counter, (unsigned long long)tot);
+    }
   }
+}
+
+// single-pass list capacity of every (group, query): children x the query's
+// parent-list length
+__global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= a.nwarps) return;
+  int lo = 0, hi = a.ngroups - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.groups[mid].qwarp_off <= w)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const GroupDesc g = a.groups[lo];
+  const long long i = w - g.qwarp_off;
+  const long long k = a.subs[g.sub_base].query_off + i;
+  long long len = 0;
+  if (GUARD_OK(a.guard, i >= 0 && i < g.nquery && k < a.prev_nkeep, 36, k)) len = a.prev_lcnt[k];
+  cap[w] = (long long)g.nchild * len;
 }
 
 // density of every (subspace, point) from its list.  The phi sum of one item
@@ -444,6 +488,9 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.lacc = L.lacc;
   a.cand_counter = L.cand_counter;
   a.list_counter = L.list_counter;
+  a.out_counter = L.out_counter;
+  a.cap_base = L.cap_base;
+  a.cap_loff = L.cap_loff;
   a.prev_total = L.prev_total;
   a.total = L.total;
   a.prev_nkeep = L.prev_nkeep;
@@ -505,6 +552,13 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
     k_neighbours_multi<true><<<blocks, 256, 0, s>>>(a);
   else
     k_neighbours_multi<false><<<blocks, 256, 0, s>>>(a);
+}
+
+void launch_list_capacity(const DensityLaunch& L, long long nwarps, long long* cap, cudaStream_t s) {
+  if (nwarps <= 0) return;
+  DensityArgs a = make_args(L);
+  a.nwarps = nwarps;
+  k_list_capacity<<<(unsigned)((nwarps + 255) / 256), 256, 0, s>>>(a, cap);
 }
 
 void launch_density_flags(const DensityLaunch& L, cudaStream_t s) {

@@ -60,7 +60,7 @@ typedef struct inscy_stats {
   double ms_total;          /* wall time of the run (host clock) */
   double ms_setup;          /* grid cells, trie order, candidate lists */
   double ms_density;        /* density kernels (pass 1 + pass 2), device time */
-  double ms_density_pass1;  /* density pass 1 alone, device time */
+  double ms_density_pass1;  /* the candidate pass alone (count pass, or the single-pass write), device time */
   double ms_tree;           /* restrict/merge/prune kernels, device time */
   double ms_cluster;        /* union-find + component kernels, device time */
   double ms_replay;         /* host commit (pruneRedundancy, numbering, join) */

@@ -71,9 +71,10 @@ def test_family_cases(driver):
 
 @pytest.fixture(scope="module")
 def driver_big_blocks():
-    # every level-kernel work item above 64 points takes the 1024-thread path
+    # every level-kernel work item above 64 points takes the 1024-thread path,
+    # and every level sizes its neighbour lists with a count pass
     import build_simt
-    return build_simt.build(defines=("INSCY_TREE_BIG=64",), tag="_treebig")
+    return build_simt.build(defines=("INSCY_TREE_BIG=64", "INSCY_SINGLE_PASS_BYTES=0"), tag="_variant")
 
 
 @pytest.fixture(scope="module")
@@ -91,7 +92,7 @@ def test_plain_workload_shape(driver, plain_case, reverse):
 
 
 @pytest.mark.parametrize("reverse", [False, True], ids=["warps-up", "warps-down"])
-def test_level_kernel_large_blocks(driver_big_blocks, plain_case, reverse):
+def test_large_blocks_and_two_pass_lists(driver_big_blocks, plain_case, reverse):
     X, p, want = plain_case
     assert_same(simt_run(driver_big_blocks, X, p, reverse, "plain_big"), want, "plain n=1000, 1024-thread items")
     X, p, want = small_case(0)
