@@ -236,10 +236,12 @@ struct LabelRef {
 // commit handles them after the calls of every smaller first dim, and a
 // superset of their subspaces either holds a smaller dim (an earlier phase)
 // or starts in the same range (this phase), so a phase can be committed as
-// soon as its expansion is done, while the GPU expands the next one.  Phase k
-// covers the first dims [2^k - 1, 2^(k+1) - 1): the lattice below dim D shrinks
-// about geometrically with D, so the early phases hold comparable work and
-// the last one, whose commit is all that is left once the GPU is done, little.
+// soon as its expansion is done, while the GPU expands the next one.  The
+// lattice below dim D shrinks quickly with D: the phases are {0}, {1}, {2},
+// {3, 4}, {5, 6, 7} and the rest, so the commit of each phase overlaps the
+// expansion of the next and the last one, whose commit is all that is left
+// once the GPU is done, holds little (a phase per dim costs the GPU more in
+// small launches than it saves).
 struct Phase {
   int d0 = 0, d1 = 0;
   std::vector<HCall> calls;    // level >= 1
@@ -699,9 +701,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   root_.npts = ni;
   phase_of_.assign(d, 0);
   for (int k = 0, d0 = 0; d0 < d; ++k) {
+    static const int kPhaseDims[] = {1, 1, 1, 2, 3};  // then the rest
     Phase ph;
     ph.d0 = d0;
-    ph.d1 = std::min(d, 2 * d0 + 1);
+    ph.d1 = k < 5 ? std::min(d, d0 + kPhaseDims[k]) : d;
     for (int D = ph.d0; D < ph.d1; ++D) phase_of_[D] = k;
     d0 = ph.d1;
     phases_.push_back(std::move(ph));
