@@ -416,89 +416,92 @@ __global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* 
           }
         }
       }
-      for (int phase = 0; phase < 2; ++phase) {
-        if (threadIdx.x == 0) {
-          if (phase == 0) s.gcount = 0;
-          s.gwrite = 0;
-        }
-        __syncthreads();
-        // (a) ghosts of points that were pruned here: the chain survives when a
-        //     kept point shares the cells of every remaining dim up to the chain's
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-          if (SV[j + 1] != SV[j]) continue;
-          int x = cur[j];
-          unsigned long long gb = a.gz[x] & lammask;
+      // The keep decisions are made once and stored in buffers free by now
+      // (the key buffer the merge sort did not end in; the chains' sort
+      // buffer), then the surviving chains are written at one reserved range.
+      unsigned long long* kmask = (unsigned long long*)(kcur == KA ? KB : KA);  // per point: chain dims kept
+      int* gkeep = GB;                                                          // per detached chain: kept
+      if (threadIdx.x == 0) {
+        s.gcount = 0;
+        s.gwrite = 0;
+      }
+      __syncthreads();
+      // (a) chains of points pruned here: a chain survives when a kept point
+      //     shares the cells of every remaining dim up to the chain's
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        unsigned long long km = 0;
+        if (SV[j + 1] == SV[j]) {
+          unsigned long long gb = a.gz[cur[j]] & lammask;
           while (gb) {
-            int g = __ffsll((long long)gb) - 1;
+            const int g = __ffsll((long long)gb) - 1;
             gb &= gb - 1;
-            int l = __popcll(lammask & ((1ull << g) - 1));
+            const int l = __popcll(lammask & ((1ull << g) - 1));
             int plo, phi;
             key_range(kcur, m, kcur[j], b * (nlam - l), plo, phi);  // prefix through level l
-            if (SV[phi] - SV[plo] > 0) {
-              if (phase == 0)
-                atomicAdd(&s.gcount, 1);
-              else {
-                int o = atomicAdd(&s.gwrite, 1);
-                if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(x, g);
-              }
-            }
+            if (SV[phi] - SV[plo] > 0) km |= 1ull << g;
           }
+          if (km) atomicAdd(&s.gcount, __popcll(km));
         }
-        // (b) ghosts detached earlier
-        for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
-          int2 gg = Gh[GA[jj]];
-          int x = gg.x, g = gg.y;
-          const Key kx = KG[jj];
-          int l = __popcll(lammask & ((1ull << g) - 1));
-          int plo, phi;
-          bool alive = true;
-          if (l > 0) {
-            key_range(kcur, m, kx, b * (nlam - l + 1), plo, phi);  // prefix through level l-1
-            alive = SV[phi] - SV[plo] > 0;
-          }
-          if (!alive) continue;
+        kmask[j] = km;
+      }
+      // (b) chains detached earlier
+      for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
+        const int2 gg = Gh[GA[jj]];
+        const int g = gg.y;
+        const Key kx = KG[jj];
+        const int l = __popcll(lammask & ((1ull << g) - 1));
+        int plo, phi;
+        bool keep = true;
+        if (l > 0) {
+          key_range(kcur, m, kx, b * (nlam - l + 1), plo, phi);  // prefix through level l-1: the parent node
+          keep = SV[phi] - SV[plo] > 0;
+        }
+        if (keep) {
           key_range(kcur, m, kx, b * (nlam - l), plo, phi);
-          bool keep;
-          if (SV[phi] - SV[plo] > 0)
+          if (SV[phi] - SV[plo] > 0) {
             keep = true;  // the sibling node keeps points
-          else if (phi > plo)
+          } else if (phi > plo) {
             keep = false;  // the sibling node existed and is erased with it
-          else {
+          } else {
             // the sibling node exists only if a deeper detached chain passes it
-            keep = true;
             int glo, ghi;
             key_range(KG, ngp, kx, b * (nlam - l), glo, ghi);
-            for (int t = glo; t < ghi; ++t) {
-              int lh = __popcll(lammask & ((1ull << Gh[GA[t]].y) - 1));
-              if (lh > l) {
+            for (int t = glo; t < ghi; ++t)
+              if (__popcll(lammask & ((1ull << Gh[GA[t]].y) - 1)) > l) {
                 keep = false;
                 break;
               }
-            }
-          }
-          if (keep) {
-            if (phase == 0)
-              atomicAdd(&s.gcount, 1);
-            else {
-              int o = atomicAdd(&s.gwrite, 1);
-              if (o < s.gcount) a.out_ghosts[s.goff + o] = gg;
-            }
           }
         }
-        __syncthreads();
-        if (phase == 0) {
-          if (threadIdx.x == 0) {
-            unsigned long long o = atomicAdd(a.out_ghost_top, (unsigned long long)s.gcount);
-            if ((long long)(o + s.gcount) > a.out_ghost_cap) {
-              atomicExch(a.err, 2);
-              s.gcount = 0;  // nothing is written; the host retries with more room
-              o = 0;
-            }
-            s.goff = (long long)o;
-          }
-          __syncthreads();
-          if (s.gcount == 0) break;
+        gkeep[jj] = keep ? 1 : 0;
+        if (keep) atomicAdd(&s.gcount, 1);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long o = atomicAdd(a.out_ghost_top, (unsigned long long)s.gcount);
+        if ((long long)(o + s.gcount) > a.out_ghost_cap) {
+          atomicExch(a.err, 2);
+          s.gcount = 0;  // nothing is written; the host retries with more room
+          o = 0;
         }
+        s.goff = (long long)o;
+      }
+      __syncthreads();
+      if (s.gcount > 0) {
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+          unsigned long long km = kmask[j];
+          while (km) {
+            const int g = __ffsll((long long)km) - 1;
+            km &= km - 1;
+            const int o = atomicAdd(&s.gwrite, 1);
+            if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(cur[j], g);
+          }
+        }
+        for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x)
+          if (gkeep[jj]) {
+            const int o = atomicAdd(&s.gwrite, 1);
+            if (o < s.gcount) a.out_ghosts[s.goff + o] = Gh[GA[jj]];
+          }
       }
       ghost_off = s.goff;
       nghost = s.gcount;
