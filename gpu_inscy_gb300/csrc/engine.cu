@@ -70,6 +70,11 @@ const double kPi = 3.14;  // ClusteringCpu.cu:27
 #define INSCY_SINGLE_PASS_BYTES (32LL << 30)
 #endif
 constexpr long long kSinglePassBytes = INSCY_SINGLE_PASS_BYTES;
+// narrowest leaf key the level kernel may use (4; raised only to test the wider forms)
+#ifndef INSCY_TREE_MIN_KEY_BYTES
+#define INSCY_TREE_MIN_KEY_BYTES 4
+#endif
+constexpr int kTreeMinKeyBytes = INSCY_TREE_MIN_KEY_BYTES;
 static float omega_of(int k) { return (float)(2.0 / ((double)k + 2.0)); }
 static float gamma_of(int m) {
   if (m == 2) return 1.0f;
@@ -1051,6 +1056,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         TL.pts_in_total = F.pts_total;
         TL.ghosts_in_total = F.ghosts_total;
         TL.guard = guard;
+        TL.key_bytes = std::max(kTreeMinKeyBytes, d * kbits <= 32 ? 4 : d * kbits <= 64 ? 8 : 16);
         TL.items_big = ditems;
         TL.nbig = ditems ? (int)items_big.size() : 0;
         TL.items_small = ditems ? ditems + items_big.size() : nullptr;

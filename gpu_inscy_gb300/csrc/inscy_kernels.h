@@ -116,6 +116,7 @@ struct TreeLaunch {
   int nbig;
   const int* items_small;
   int nsmall;
+  int key_bytes;  // leaf key width: 4, 8 or 16 bytes (d * kbits bits must fit)
 };
 #ifndef INSCY_TREE_BIG
 #define INSCY_TREE_BIG 4096

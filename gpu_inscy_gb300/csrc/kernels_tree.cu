@@ -45,7 +45,10 @@ namespace inscy {
 constexpr int kTreeThreads = 256;
 constexpr int kTreeThreadsBig = 1024;
 
-using Key = unsigned __int128;
+// Leaf keys: one cell per dim, kbits bits each; the engine picks the
+// narrowest of 32, 64 and 128 bits that holds d * kbits (wide shifts and
+// compares cost several instructions each).
+using Key128 = unsigned __int128;
 
 struct TreeArgs {
   const CallDesc* calls;
@@ -94,7 +97,7 @@ __device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) 
 
 // one stable counting-sort pass of (key, value) pairs by an 8-bit digit of
 // the key (warp match for the intra-warp rank, block scan across warps)
-template <int kWarps>
+template <int kWarps, class Key>
 __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* vout, int n, int shift, int* s_base,
                                 int* s_tot, int* s_wc) {
   const int R = 256;
@@ -175,6 +178,7 @@ struct TreeShared {
 
 // leaf key of point x: its cells on the remaining dims (in level order, most
 // significant first), then its cell on the restricted dim D
+template <class Key>
 __device__ __forceinline__ Key leaf_key(const uint8_t* cc, int d, const int* lam, int nlam, int D, int b, int x) {
   const uint8_t* row = cc + (size_t)x * d;
   Key k = 0;
@@ -183,6 +187,7 @@ __device__ __forceinline__ Key leaf_key(const uint8_t* cc, int d, const int* lam
 }
 
 // [lo, hi) of the keys of K[0..m) that share `key`'s prefix above bit `sh`
+template <class Key>
 __device__ __forceinline__ void key_range(const Key* K, int m, Key key, int sh, int& lo, int& hi) {
   const Key pre = key >> sh;
   int a = 0, b = m;
@@ -206,8 +211,8 @@ __device__ __forceinline__ void key_range(const Key* K, int m, Key key, int sh, 
 }
 
 // one block per work item: items[blockIdx.x], or blockIdx.x without a list
-template <int kThreads>
-__global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* __restrict__ items, int nitems) {
+template <int kThreads, class Key>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeArgs a, const int* __restrict__ items, int nitems) {
   __shared__ TreeShared<kThreads / 32> s;
   if ((int)blockIdx.x >= nitems) return;
   const int w = items ? items[blockIdx.x] : (int)blockIdx.x;
@@ -239,11 +244,13 @@ __global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* 
   const unsigned* wd = a.bitmaps + S.bitmap_off;
   // scratch: keys first (16-byte aligned), then ints
   char* base = a.scratch + a.work_scratch[w];
-  Key* KA = (Key*)base;  // np: leaf keys of the region's points
-  Key* KB = KA + np;     // np
-  Key* KG = KB + np;     // ng: leaf keys of the region's detached chains
-  Key* KH = KG + ng;     // ng
-  int* A = (int*)(KH + ng);  // np: the region's points
+  // key buffers in 16-byte slots whatever the key width (a free one holds
+  // 8-byte chain masks later)
+  Key* KA = (Key*)base;                              // np: leaf keys of the region's points
+  Key* KB = (Key*)(base + 16LL * np);                // np
+  Key* KG = (Key*)(base + 32LL * np);                // ng: leaf keys of the region's detached chains
+  Key* KH = (Key*)(base + 32LL * np + 16LL * ng);    // ng
+  int* A = (int*)(base + 32LL * (np + ng));  // np: the region's points
   int* B = A + np;
   int* SV = B + np;       // np + 1 survivor prefix counts
   int* GA = SV + np + 1;  // ng: detached chains of the region
@@ -315,7 +322,7 @@ __global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* 
             return c >= c0 && c <= c1;
           },
           A, s.sh);
-    for (int j = threadIdx.x; j < m; j += blockDim.x) KA[j] = leaf_key(a.cc, d, s.lam, nlam, D, b, A[j]);
+    for (int j = threadIdx.x; j < m; j += blockDim.x) KA[j] = leaf_key<Key>(a.cc, d, s.lam, nlam, D, b, A[j]);
     __syncthreads();
     // 4. merged runs: stable re-sort by the leaf key (remaining cells, cell on
     //    D); equal keys keep their order (the restricted dims, then id)
@@ -391,7 +398,7 @@ __global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* 
           ngp += tot;
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < ngp; j += blockDim.x) KG[j] = leaf_key(a.cc, d, s.lam, nlam, D, b, Gh[GA[j]].x);
+        for (int j = threadIdx.x; j < ngp; j += blockDim.x) KG[j] = leaf_key<Key>(a.cc, d, s.lam, nlam, D, b, Gh[GA[j]].x);
         __syncthreads();
         if (ngp > 1) {
           Key* kc = KG;
@@ -525,6 +532,16 @@ __global__ void __launch_bounds__(kThreads) k_tree_level(TreeArgs a, const int* 
   if (threadIdx.x == 0) a.nrecs[w] = nruns;
 }
 
+template <class Key>
+static void tree_launches(const TreeArgs& a, const TreeLaunch& L, cudaStream_t s) {
+  if (L.nbig > 0) {
+    k_tree_level<kTreeThreadsBig, Key><<<L.nbig, kTreeThreadsBig, 0, s>>>(a, L.items_big, L.nbig);
+    if (L.nsmall > 0) k_tree_level<kTreeThreads, Key><<<L.nsmall, kTreeThreads, 0, s>>>(a, L.items_small, L.nsmall);
+  } else {
+    k_tree_level<kTreeThreads, Key><<<L.nwork, kTreeThreads, 0, s>>>(a, nullptr, L.nwork);
+  }
+}
+
 void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
   if (L.nwork <= 0) return;
   TreeArgs a;
@@ -557,12 +574,12 @@ void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
   a.pts_in_total = L.pts_in_total;
   a.ghosts_in_total = L.ghosts_in_total;
   a.guard = L.guard;
-  if (L.nbig > 0) {
-    k_tree_level<kTreeThreadsBig><<<L.nbig, kTreeThreadsBig, 0, s>>>(a, L.items_big, L.nbig);
-    if (L.nsmall > 0) k_tree_level<kTreeThreads><<<L.nsmall, kTreeThreads, 0, s>>>(a, L.items_small, L.nsmall);
-  } else {
-    k_tree_level<kTreeThreads><<<L.nwork, kTreeThreads, 0, s>>>(a, nullptr, L.nwork);
-  }
+  if (L.key_bytes <= 4)
+    tree_launches<uint32_t>(a, L, s);
+  else if (L.key_bytes <= 8)
+    tree_launches<unsigned long long>(a, L, s);
+  else
+    tree_launches<Key128>(a, L, s);
 }
 
 }  // namespace inscy

@@ -72,9 +72,17 @@ def test_family_cases(driver):
 @pytest.fixture(scope="module")
 def driver_big_blocks():
     # every level-kernel work item above 64 points takes the 1024-thread path,
-    # and every level sizes its neighbour lists with a count pass
+    # every level sizes its neighbour lists with a count pass, and the leaf
+    # keys are 128 bits wide
     import build_simt
-    return build_simt.build(defines=("INSCY_TREE_BIG=64", "INSCY_SINGLE_PASS_BYTES=0"), tag="_variant")
+    return build_simt.build(defines=("INSCY_TREE_BIG=64", "INSCY_SINGLE_PASS_BYTES=0", "INSCY_TREE_MIN_KEY_BYTES=16"),
+                            tag="_variant")
+
+
+@pytest.fixture(scope="module")
+def driver_key64():
+    import build_simt
+    return build_simt.build(defines=("INSCY_TREE_MIN_KEY_BYTES=8",), tag="_key64")
 
 
 @pytest.fixture(scope="module")
@@ -92,8 +100,13 @@ def test_plain_workload_shape(driver, plain_case, reverse):
 
 
 @pytest.mark.parametrize("reverse", [False, True], ids=["warps-up", "warps-down"])
-def test_large_blocks_and_two_pass_lists(driver_big_blocks, plain_case, reverse):
+def test_large_blocks_two_pass_lists_wide_keys(driver_big_blocks, plain_case, reverse):
     X, p, want = plain_case
     assert_same(simt_run(driver_big_blocks, X, p, reverse, "plain_big"), want, "plain n=1000, 1024-thread items")
     X, p, want = small_case(0)
     assert_same(simt_run(driver_big_blocks, X, p, reverse, "small_big"), want, "small, 1024-thread items")
+
+
+def test_64_bit_leaf_keys(driver_key64, plain_case):
+    X, p, want = plain_case
+    assert_same(simt_run(driver_key64, X, p, True, "plain_key64"), want, "plain n=1000, 64-bit keys")
