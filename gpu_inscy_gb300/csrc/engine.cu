@@ -1559,9 +1559,9 @@ bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
 void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState& st) {
   const HSub& hs = ph.subs[c.csub];
   const int* order = level_of(ph, c).order.data() + c.order_off;
-  // labels in first-seed order.  Components are disjoint and their border
-  // points are not dense, so no write below changes another component's
-  // first member: all labels can be decided before the writes.
+  // labels in first-seed order.  Components are disjoint, so no write below
+  // changes another component's first member: all labels can be decided
+  // before the writes.
   const int first = st.nlabels + 1;
   long long work = 0;
   for (int t = 0; t < c.norder; ++t) {
@@ -1574,42 +1574,35 @@ void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState
     rc_[9] += hs.boff[comp + 1] - hs.boff[comp];
     st.ref.push_back(LabelRef{&hs, comp});
     st.size.push_back((int)(m1 - m0));
-    work += (m1 - m0) + (hs.boff[comp + 1] - hs.boff[comp]);
+    if (m1 - m0 >= hp_.min_size) work += m1 - m0;
   }
-  // members get the label; non-dense neighbours that are still -1 become -2
-  // (the only other value they can hold here)
-  if (work < kParallelWalk || hpool_->workers() == 0) {
-    for (int label = first; label <= st.nlabels; ++label) {
-      const int comp = st.ref[label].comp;
-      for (long long k = hs.moff[comp]; k < hs.moff[comp + 1]; ++k) V.set(hs.members[k], label);
-      for (long long k = hs.boff[comp]; k < hs.boff[comp + 1]; ++k) {
-        const int q = hs.borders[k];
-        if (V.get(q) == -1) V.set(q, -2);
-      }
-    }
-    return;
-  }
+  // The loop vector is read in two places only: the check above (a
+  // component's first member) and join's redundancy test, which looks at
+  // clusters of min_size points or more (smaller ones are dropped first).  So
+  // those clusters get every member labelled and the others their first
+  // member; the -2 marks of border points reach the result entry from the
+  // component lists in join and are never read from the loop vector.
+  uint64_t* gv = V.gv.data();
+  const uint64_t cur = V.cur;
   pieces_.clear();
   for (int label = first; label <= st.nlabels; ++label) {
     const int comp = st.ref[label].comp;
-    pieces_.push_back(Walk{hs.members.data() + hs.moff[comp], 0, hs.moff[comp + 1] - hs.moff[comp], nullptr, label, 0.f});
-    pieces_.push_back(Walk{hs.borders.data() + hs.boff[comp], 0, hs.boff[comp + 1] - hs.boff[comp], nullptr, -2, 0.f});
+    const long long m0 = hs.moff[comp], m = hs.moff[comp + 1] - m0;
+    if (m >= hp_.min_size && m > 1)
+      pieces_.push_back(Walk{hs.members.data() + m0, 0, m, nullptr, label, 0.f});
+    else
+      gv[hs.members[m0]] = cur | (uint32_t)label;
   }
-  uint64_t* gv = V.gv.data();
-  const uint64_t cur = V.cur;
-  split_pieces(work);
-  hpool_->run((int)split_.size(), [&](int i) {
-    const Walk& w = split_[i];
+  auto write = [&](const Walk& w) {
     const uint64_t v = cur | (uint32_t)w.l;
-    if (w.l > 0) {
-      for (long long k = w.k0; k < w.k1; ++k) __atomic_store_n(&gv[w.mem[k]], v, __ATOMIC_RELAXED);
-    } else {
-      for (long long k = w.k0; k < w.k1; ++k) {
-        uint64_t* g = &gv[w.mem[k]];
-        if ((__atomic_load_n(g, __ATOMIC_RELAXED) & 0xffffffff00000000ull) != cur) __atomic_store_n(g, v, __ATOMIC_RELAXED);
-      }
-    }
-  });
+    for (long long k = w.k0; k < w.k1; ++k) __atomic_store_n(&gv[w.mem[k]], v, __ATOMIC_RELAXED);
+  };
+  if (work < kParallelWalk || hpool_->workers() == 0) {
+    for (const Walk& w : pieces_) write(w);
+    return;
+  }
+  split_pieces(work);
+  hpool_->run((int)split_.size(), [&](int i) { write(split_[i]); });
 }
 
 // pieces_ cut into parts of about work / (4 * threads) entries (split_)
@@ -1651,6 +1644,12 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       rc_[4]++;
       if (!((float)minsz * hp_.r < (float)H.maxsz)) continue;
       refresh_order(H);
+      // The test can walk either side: the points of H's clusters larger than
+      // (smallest cluster here) * r, against the loop vector, or the members
+      // of the clusters here that some cluster of H can drop, against H's
+      // labels (stopping at a cluster's first hit).  Take the shorter.
+      const size_t w0 = walk_.size();
+      long long cost_h = 0, cost_here = 0;
       for (int t = (int)H.by_size.size() - 1; t >= 0; --t) {
         const int l = H.by_size[t];
         const int hsz = H.size[l];
@@ -1659,7 +1658,38 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         const int cp = H.src[l].comp;
         const long long m = hs.moff[cp + 1] - hs.moff[cp];
         walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, m, H.lab.data(), l, (float)hsz});
-        total += m;
+        cost_h += m;
+      }
+      for (int c = 1; c <= nl; ++c)
+        if (alive[c] && (float)st.size[c] * hp_.r < (float)H.maxsz) cost_here += st.size[c];
+      if (cost_here < cost_h) {
+        walk_.resize(w0);
+        rc_[5] += cost_here;
+        const int* hl = H.lab.data();
+        const int* hsize = H.size.data();
+        bool hit = false;
+        for (int c = 1; c <= nl; ++c) {
+          const float csz = (float)st.size[c] * hp_.r;
+          if (!alive[c] || !(csz < (float)H.maxsz)) continue;
+          const HSub& hs = *st.ref[c].hs;
+          const int cp = st.ref[c].comp;
+          for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+            const int l = hl[hs.members[k]];
+            if (l >= 0 && csz < (float)hsize[l]) {
+              alive[c] = 0;
+              hit = true;
+              break;
+            }
+          }
+        }
+        if (hit) {
+          minsz = INT32_MAX;
+          for (int l = 1; l <= nl; ++l)
+            if (alive[l]) minsz = std::min(minsz, st.size[l]);
+          if (minsz == INT32_MAX) return;
+        }
+      } else {
+        total += cost_h;
       }
     }
     rc_[5] += total;
