@@ -367,19 +367,35 @@ class HostPool {
   bool stop_ = false;
 };
 
-// Points [k0, k1) of a superset cluster's member list (the points still
-// labelled l in that entry count) for join's redundancy test.
+// Points [k0, k1) of a member list for join's redundancy test.  Without
+// `hsize`: members of a superset cluster (those still labelled l in that
+// entry's `lab` count), tested against the loop vector, hsz = its size.  With
+// `hsize`: members of cluster l here, tested against a superset entry's labels
+// `lab` and cluster sizes `hsize`, hsz = size(l) * r.  Elsewhere: a range of
+// points to label l.
 struct Walk {
   const int* mem;
   long long k0, k1;
   const int* lab;
   int l;
   float hsz;
+  const int* hsize = nullptr;
 };
 
 // Drop every live cluster c of the loop with a point in w and
 // size(c) * r < |w's cluster| (util.cu:680-705); true if one was dropped.
 static bool walk_test(const Walk& w, const LoopVec& V, const int* size, float r, char* alive) {
+  if (w.hsize) {  // the cluster here against the superset entry's clusters
+    if (!__atomic_load_n(&alive[w.l], __ATOMIC_RELAXED)) return false;
+    for (long long k = w.k0; k < w.k1; ++k) {
+      const int h = w.lab[w.mem[k]];
+      if (h >= 0 && w.hsz < (float)w.hsize[h]) {
+        __atomic_store_n(&alive[w.l], (char)0, __ATOMIC_RELAXED);
+        return true;
+      }
+    }
+    return false;
+  }
   bool hit = false;
   const uint64_t* gv = V.gv.data();
   const uint64_t cur = V.cur;
@@ -1610,7 +1626,8 @@ void Engine::split_pieces(long long work) {
   split_.clear();
   const long long part = std::max(4096LL, work / (4LL * (hpool_->workers() + 1)));
   for (const Walk& w : pieces_)
-    for (long long k = w.k0; k < w.k1; k += part) split_.push_back(Walk{w.mem, k, std::min(w.k1, k + part), w.lab, w.l, w.hsz});
+    for (long long k = w.k0; k < w.k1; k += part)
+      split_.push_back(Walk{w.mem, k, std::min(w.k1, k + part), w.lab, w.l, w.hsz, w.hsize});
 }
 
 // join (util.cu:655-743): drop clusters below min_size, drop clusters a
@@ -1664,30 +1681,15 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         if (alive[c] && (float)st.size[c] * hp_.r < (float)H.maxsz) cost_here += st.size[c];
       if (cost_here < cost_h) {
         walk_.resize(w0);
-        rc_[5] += cost_here;
-        const int* hl = H.lab.data();
-        const int* hsize = H.size.data();
-        bool hit = false;
         for (int c = 1; c <= nl; ++c) {
           const float csz = (float)st.size[c] * hp_.r;
           if (!alive[c] || !(csz < (float)H.maxsz)) continue;
           const HSub& hs = *st.ref[c].hs;
           const int cp = st.ref[c].comp;
-          for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
-            const int l = hl[hs.members[k]];
-            if (l >= 0 && csz < (float)hsize[l]) {
-              alive[c] = 0;
-              hit = true;
-              break;
-            }
-          }
+          walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, hs.moff[cp + 1] - hs.moff[cp], H.lab.data(), c, csz,
+                               H.size.data()});
         }
-        if (hit) {
-          minsz = INT32_MAX;
-          for (int l = 1; l <= nl; ++l)
-            if (alive[l]) minsz = std::min(minsz, st.size[l]);
-          if (minsz == INT32_MAX) return;
-        }
+        total += cost_here;
       } else {
         total += cost_h;
       }
@@ -1699,7 +1701,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     if (total < kParallelWalk || hpool_->workers() == 0) {
       // one thread: raise the size bar as clusters drop
       for (const Walk& w : walk_) {
-        if (!((float)minsz * r < w.hsz)) continue;
+        if (!w.hsize && !((float)minsz * r < w.hsz)) continue;
         if (walk_test(w, V, ssz, r, alive.data())) {
           hit = true;
           minsz = INT32_MAX;
