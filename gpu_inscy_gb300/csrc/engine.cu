@@ -367,35 +367,20 @@ class HostPool {
   bool stop_ = false;
 };
 
-// Points [k0, k1) of a member list for join's redundancy test.  Without
-// `hsize`: members of a superset cluster (those still labelled l in that
-// entry's `lab` count), tested against the loop vector, hsz = its size.  With
-// `hsize`: members of cluster l here, tested against a superset entry's labels
-// `lab` and cluster sizes `hsize`, hsz = size(l) * r.  Elsewhere: a range of
-// points to label l.
+// Points [k0, k1) of a member list: for join's redundancy test the members of
+// a superset cluster (those still labelled l in that entry's `lab` count, hsz
+// = its size); elsewhere a range of points to label l.
 struct Walk {
   const int* mem;
   long long k0, k1;
   const int* lab;
   int l;
   float hsz;
-  const int* hsize = nullptr;
 };
 
 // Drop every live cluster c of the loop with a point in w and
 // size(c) * r < |w's cluster| (util.cu:680-705); true if one was dropped.
 static bool walk_test(const Walk& w, const LoopVec& V, const int* size, float r, char* alive) {
-  if (w.hsize) {  // the cluster here against the superset entry's clusters
-    if (!__atomic_load_n(&alive[w.l], __ATOMIC_RELAXED)) return false;
-    for (long long k = w.k0; k < w.k1; ++k) {
-      const int h = w.lab[w.mem[k]];
-      if (h >= 0 && w.hsz < (float)w.hsize[h]) {
-        __atomic_store_n(&alive[w.l], (char)0, __ATOMIC_RELAXED);
-        return true;
-      }
-    }
-    return false;
-  }
   bool hit = false;
   const uint64_t* gv = V.gv.data();
   const uint64_t cur = V.cur;
@@ -1627,7 +1612,7 @@ void Engine::split_pieces(long long work) {
   const long long part = std::max(4096LL, work / (4LL * (hpool_->workers() + 1)));
   for (const Walk& w : pieces_)
     for (long long k = w.k0; k < w.k1; k += part)
-      split_.push_back(Walk{w.mem, k, std::min(w.k1, k + part), w.lab, w.l, w.hsz, w.hsize});
+      split_.push_back(Walk{w.mem, k, std::min(w.k1, k + part), w.lab, w.l, w.hsz});
 }
 
 // join (util.cu:655-743): drop clusters below min_size, drop clusters a
@@ -1661,12 +1646,6 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       rc_[4]++;
       if (!((float)minsz * hp_.r < (float)H.maxsz)) continue;
       refresh_order(H);
-      // The test can walk either side: the points of H's clusters larger than
-      // (smallest cluster here) * r, against the loop vector, or the members
-      // of the clusters here that some cluster of H can drop, against H's
-      // labels (stopping at a cluster's first hit).  Take the shorter.
-      const size_t w0 = walk_.size();
-      long long cost_h = 0, cost_here = 0;
       for (int t = (int)H.by_size.size() - 1; t >= 0; --t) {
         const int l = H.by_size[t];
         const int hsz = H.size[l];
@@ -1675,23 +1654,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         const int cp = H.src[l].comp;
         const long long m = hs.moff[cp + 1] - hs.moff[cp];
         walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, m, H.lab.data(), l, (float)hsz});
-        cost_h += m;
-      }
-      for (int c = 1; c <= nl; ++c)
-        if (alive[c] && (float)st.size[c] * hp_.r < (float)H.maxsz) cost_here += st.size[c];
-      if (cost_here < cost_h) {
-        walk_.resize(w0);
-        for (int c = 1; c <= nl; ++c) {
-          const float csz = (float)st.size[c] * hp_.r;
-          if (!alive[c] || !(csz < (float)H.maxsz)) continue;
-          const HSub& hs = *st.ref[c].hs;
-          const int cp = st.ref[c].comp;
-          walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, hs.moff[cp + 1] - hs.moff[cp], H.lab.data(), c, csz,
-                               H.size.data()});
-        }
-        total += cost_here;
-      } else {
-        total += cost_h;
+        total += m;
       }
     }
     rc_[5] += total;
@@ -1701,7 +1664,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     if (total < kParallelWalk || hpool_->workers() == 0) {
       // one thread: raise the size bar as clusters drop
       for (const Walk& w : walk_) {
-        if (!w.hsize && !((float)minsz * r < w.hsz)) continue;
+        if (!((float)minsz * r < w.hsz)) continue;
         if (walk_test(w, V, ssz, r, alive.data())) {
           hit = true;
           minsz = INT32_MAX;
