@@ -21,7 +21,7 @@ MODE_PLAIN = 0
 MODE_BATCHED = 1
 
 # every symbol include/inscy_gb300.h declares
-EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_result_count", "inscy_result_n",
+EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_run_batch_scheduled", "inscy_result_count", "inscy_result_n",
            "inscy_result_subspace", "inscy_result_labels", "inscy_result_labels_ptr", "inscy_result_stats",
            "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest", "inscy_selftest_noalloc"]
 
@@ -161,12 +161,20 @@ def run_device(ptr, n, d, params, stream=0, mode=MODE_PLAIN):
     return collect(h)
 
 
-def run_batch(Xs, params, mode=MODE_BATCHED):
+def run_batch(Xs, params, mode=MODE_BATCHED, order=None, lanes=None):
+    """Many datasets: mode PLAIN one after another; BATCHED on concurrent lanes,
+    taking the datasets in `order` (default 0, 1, ...) over `lanes` lanes
+    (default 4).  Returns one (subspaces, labels, stats) per dataset, in input order."""
     Xs = [np.ascontiguousarray(x, dtype=np.float32) for x in Xs]
     B = len(Xs)
     ptrs = (ctypes.c_void_p * B)(*[x.ctypes.data for x in Xs])
     ns = (ctypes.c_int64 * B)(*[x.shape[0] for x in Xs])
     ds = (ctypes.c_int * B)(*[x.shape[1] for x in Xs])
     outs = (ctypes.c_void_p * B)()
-    check(load().inscy_run_batch(ptrs, ns, ds, B, ctypes.byref(params), mode, outs))
+    if mode == MODE_BATCHED and (order is not None or lanes is not None):
+        ordp = None if order is None else (ctypes.c_int * B)(*[int(i) for i in order])
+        check(load().inscy_run_batch_scheduled(ptrs, ns, ds, B, ctypes.byref(params), ordp,
+                                               int(lanes if lanes is not None else 4), outs))
+    else:
+        check(load().inscy_run_batch(ptrs, ns, ds, B, ctypes.byref(params), mode, outs))
     return [collect(outs[i]) for i in range(B)]

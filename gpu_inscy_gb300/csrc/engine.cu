@@ -406,6 +406,10 @@ struct HostParams {
   int num_obj, min_size, cells, rect;
 };
 
+// host-pool workers of engines created on this thread (-1: by the core count;
+// batch lanes set it so that concurrent engines share the cores)
+thread_local int t_pool_workers = -1;
+
 // ---------------------------------------------------------------------------
 // the engine (one run at a time; device resources are kept between runs)
 // ---------------------------------------------------------------------------
@@ -416,7 +420,7 @@ class Engine {
     pool_.reset(new Pool(device_));
     {
       const int hw = (int)std::thread::hardware_concurrency();
-      hpool_.reset(new HostPool(std::max(0, std::min(7, hw / 2 - 1))));
+      hpool_.reset(new HostPool(t_pool_workers >= 0 ? t_pool_workers : std::max(0, std::min(7, hw / 2 - 1))));
     }
     CK(cudaEventCreate(&ev0_));
     CK(cudaEventCreate(&ev1_));
@@ -1896,6 +1900,85 @@ int run_common(const float* X, bool on_device, int64_t n, int d, const inscy_par
     return fail(INSCY_ERR_INTERNAL, e.what());
   }
 }
+// Batch lanes: host threads that each own an engine (memory pool, events,
+// commit thread) and a non-blocking CUDA stream, so that several datasets
+// run at once -- their kernels overlap on the GPU and their commits on the
+// host cores.  A lane takes the next dataset of the schedule when its last
+// one is done.  The lanes stay parked between calls (engines keep their
+// warmed pools); a call with another device or lane count makes a new set.
+struct BatchJob {
+  const float* X;
+  int64_t n;
+  int d;
+  inscy_result** out;
+  int rc;
+  std::string err;
+};
+
+class LanePool {
+ public:
+  LanePool(int device, int lanes) : device_(device), lanes_(lanes) {
+    for (int i = 0; i < lanes; ++i) th_.emplace_back([this] { lane_main(); });
+    for (auto& t : th_) t.detach();  // parked until exit
+  }
+  int device() const { return device_; }
+  int lanes() const { return lanes_; }
+  void run(std::vector<BatchJob>& jobs, const inscy_params* p) {
+    std::unique_lock<std::mutex> lk(m_);
+    jobs_ = &jobs;
+    p_ = p;
+    next_ = 0;
+    active_ = lanes_;
+    ++gen_;
+    cv_.notify_all();
+    done_.wait(lk, [&] { return active_ == 0; });
+    jobs_ = nullptr;
+  }
+
+ private:
+  void lane_main() {
+    cudaSetDevice(device_);
+    const int hw = (int)std::thread::hardware_concurrency();
+    inscy::t_pool_workers = std::max(0, std::min(7, hw / (2 * lanes_) - 1));
+    cudaStream_t s = nullptr;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    long long seen = 0;
+    for (;;) {
+      std::vector<BatchJob>* jobs;
+      const inscy_params* p;
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        jobs = jobs_;
+        p = p_;
+      }
+      for (;;) {
+        const int i = next_.fetch_add(1);
+        if (i >= (int)jobs->size()) break;
+        BatchJob& j = (*jobs)[i];
+        j.rc = run_common(j.X, false, j.n, j.d, p, s, j.out);
+        if (j.rc) j.err = g_err;
+      }
+      std::lock_guard<std::mutex> lk(m_);
+      if (--active_ == 0) done_.notify_all();
+    }
+  }
+  int device_, lanes_;
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  std::vector<BatchJob>* jobs_ = nullptr;
+  const inscy_params* p_ = nullptr;
+  std::atomic<int> next_{0};
+  int active_ = 0;
+  long long gen_ = 0;
+};
+
+std::mutex g_lanes_m;
+LanePool* g_lanes = nullptr;  // the current lane set (earlier sets stay parked)
+
+constexpr int kDefaultLanes = 4;
 }  // namespace
 
 extern "C" {
@@ -1911,8 +1994,43 @@ int inscy_run_device(const float* X_dev, int64_t n, int d, const inscy_params* p
   return run_common(X_dev, true, n, d, p, stream, out);
 }
 
+int inscy_run_batch_scheduled(const float* const* Xs, const int64_t* ns, const int* ds, int count,
+                              const inscy_params* p, const int* order, int lanes, inscy_result** outs) {
+  if (count < 0 || (count > 0 && (!Xs || !ns || !ds || !outs))) return fail(INSCY_ERR_ARG, "bad batch arguments");
+  if (lanes < 1 || lanes > 64) return fail(INSCY_ERR_ARG, "lanes must be in [1, 64]");
+  for (int i = 0; i < count; ++i) outs[i] = nullptr;
+  if (count == 0) return INSCY_OK;
+  std::vector<char> seen(count, 0);
+  std::vector<BatchJob> jobs(count);
+  for (int k = 0; k < count; ++k) {
+    const int i = order ? order[k] : k;
+    if (i < 0 || i >= count || seen[i]) return fail(INSCY_ERR_ARG, "order is not a permutation of 0..count-1");
+    seen[i] = 1;
+    jobs[k] = BatchJob{Xs[i], ns[i], ds[i], &outs[i], 0, std::string()};
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(INSCY_ERR_CUDA, "cudaGetDevice failed");
+  {
+    std::lock_guard<std::mutex> g(g_lanes_m);  // one scheduled batch at a time per process
+    if (!g_lanes || g_lanes->device() != dev || g_lanes->lanes() != lanes) g_lanes = new LanePool(dev, lanes);
+    g_lanes->run(jobs, p);
+  }
+  for (const BatchJob& j : jobs)
+    if (j.rc) {
+      for (int i = 0; i < count; ++i) {
+        delete outs[i];
+        outs[i] = nullptr;
+      }
+      return fail(j.rc, j.err);
+    }
+  g_err.clear();
+  return INSCY_OK;
+}
+
 int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, int count, const inscy_params* p,
                     int mode, inscy_result** outs) {
+  if (mode == INSCY_MODE_BATCHED)
+    return inscy_run_batch_scheduled(Xs, ns, ds, count, p, nullptr, std::max(1, std::min(kDefaultLanes, count)), outs);
   if (count < 0 || (count > 0 && (!Xs || !ns || !ds || !outs))) return fail(INSCY_ERR_ARG, "bad batch arguments");
   for (int i = 0; i < count; ++i) outs[i] = nullptr;
   for (int i = 0; i < count; ++i) {

@@ -48,9 +48,9 @@ typedef struct inscy_params {
   int entropy_order;       /* dim order of the tree (inscy_map.cpp:61-121); only 0 is supported */
 } inscy_params;
 
-/* Execution form.  PLAIN: one level of the subspace lattice at a time, with
- * per-level kernels.  BATCHED: the same result through the batched path (all
- * datasets of an inscy_run_batch call share each level's launches). */
+/* Execution form of inscy_run_batch.  PLAIN: the datasets one after another.
+ * BATCHED: the datasets on concurrent lanes (inscy_run_batch_scheduled with
+ * the given order and 4 lanes).  Results are the same either way. */
 enum { INSCY_MODE_PLAIN = 0, INSCY_MODE_BATCHED = 1 };
 
 typedef struct inscy_result inscy_result;
@@ -104,6 +104,17 @@ int inscy_run_device(const float* X_dev, int64_t n, int d, const inscy_params* p
  * inscy_run. */
 int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, int count, const inscy_params* p,
                     int mode, inscy_result** outs);
+
+/* The batched form (no counterpart in the reference, whose batched runs are
+ * sequential): `lanes` host threads, each with its own engine and CUDA
+ * stream, run the datasets concurrently -- their kernels overlap on the GPU
+ * and their ordered commits on the host cores.  Each lane takes the next
+ * dataset of `order` (a permutation of 0..count-1; NULL: 0, 1, ...), so the
+ * order is the schedule (a cost model can put the longest datasets first).
+ * outs[i] receives the result of Xs[i], identical to inscy_run's.  1 <= lanes
+ * <= 64.  Calls are serialised within a process. */
+int inscy_run_batch_scheduled(const float* const* Xs, const int64_t* ns, const int* ds, int count,
+                              const inscy_params* p, const int* order, int lanes, inscy_result** outs);
 
 /* Result access. */
 int inscy_result_count(const inscy_result* r);              /* number of clustered subspaces */

@@ -121,6 +121,30 @@ def test_batch_entry(engine):
         assert_same((subs, labels), orc.run(X, **p), "batch")
 
 
+@pytest.mark.parametrize("lanes", [1, 3, 8])
+def test_scheduled_batch_equals_plain_runs(engine, lanes):
+    # concurrent lanes, any schedule: every dataset's result is its plain run's
+    rng = np.random.default_rng(5)
+    Xs = [synth.make_random(40 + s, int(rng.integers(200, 3000)), int(rng.integers(3, 9)), n_clusters=3, std=0.04)
+          for s in range(10)]
+    p = dict(neighborhood_size=0.08, F=1.0, num_obj=3, min_size=10, r=1.0, number_of_cells=4)
+    params = _lib.make_params(**p)
+    want = [_lib.run_host(X, params)[:2] for X in Xs]
+    order = list(rng.permutation(len(Xs)))
+    got = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, order=order, lanes=lanes)
+    for i, (w, g) in enumerate(zip(want, got)):
+        assert_same(g[:2], w, "dataset %d, %d lanes" % (i, lanes))
+    got = _lib.run_batch(Xs, params, _lib.MODE_BATCHED)  # default schedule and lanes
+    for i, (w, g) in enumerate(zip(want, got)):
+        assert_same(g[:2], w, "dataset %d, default lanes" % i)
+
+
+def test_scheduled_batch_rejects_bad_order(engine):
+    Xs = [synth.make_random(1, 100, 3), synth.make_random(2, 100, 3)]
+    with pytest.raises(_lib.InscyError):
+        _lib.run_batch(Xs, _lib.make_params(**BASE), _lib.MODE_BATCHED, order=[0, 0], lanes=2)
+
+
 # ---------------------------------------------------------------- edge cases
 BASE = dict(neighborhood_size=0.1, F=1.0, num_obj=2, min_size=3, r=1.0, number_of_cells=4)
 
