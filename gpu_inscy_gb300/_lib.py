@@ -23,7 +23,8 @@ MODE_BATCHED = 1
 # every symbol include/inscy_gb300.h declares
 EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_run_batch_scheduled", "inscy_result_count", "inscy_result_n",
            "inscy_result_subspace", "inscy_result_labels", "inscy_result_labels_ptr", "inscy_result_stats",
-           "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest", "inscy_selftest_noalloc"]
+           "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest", "inscy_selftest_noalloc",
+           "inscy_mlp_params", "inscy_mlp_train", "inscy_mlp_predict", "inscy_mlp_grad", "inscy_mlp_last_error"]
 
 
 class Params(ctypes.Structure):
@@ -73,6 +74,15 @@ def load():
     lib.inscy_run_device.argtypes = [vp, i64, c_int, ctypes.POINTER(Params), c_int, vp, ctypes.POINTER(vp)]
     lib.inscy_run_batch.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(c_int), c_int,
                                     ctypes.POINTER(Params), c_int, ctypes.POINTER(vp)]
+    lib.inscy_run_batch_scheduled.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(c_int), c_int,
+                                              ctypes.POINTER(Params), ctypes.POINTER(c_int), c_int,
+                                              ctypes.POINTER(vp)]
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.inscy_mlp_params.argtypes = [c_int, c_int]
+    lib.inscy_mlp_train.argtypes = [fp, c_int, c_int, fp, fp, c_int, c_int, ctypes.c_float, fp]
+    lib.inscy_mlp_predict.argtypes = [fp, c_int, c_int, fp, c_int, fp]
+    lib.inscy_mlp_grad.argtypes = [fp, c_int, c_int, fp, fp, c_int, fp, fp]
+    lib.inscy_mlp_last_error.restype = ctypes.c_char_p
     lib.inscy_result_count.argtypes = [vp]
     lib.inscy_result_n.argtypes = [vp]
     lib.inscy_result_n.restype = i64
@@ -173,8 +183,54 @@ def run_batch(Xs, params, mode=MODE_BATCHED, order=None, lanes=None):
     outs = (ctypes.c_void_p * B)()
     if mode == MODE_BATCHED and (order is not None or lanes is not None):
         ordp = None if order is None else (ctypes.c_int * B)(*[int(i) for i in order])
-        check(load().inscy_run_batch_scheduled(ptrs, ns, ds, B, ctypes.byref(params), ordp,
+        check(load().inscy_run_batch_scheduled(ptrs, ns, ds, B, ctypes.byref(params),
+                                               ctypes.cast(ordp, ctypes.POINTER(ctypes.c_int)),
                                                int(lanes if lanes is not None else 4), outs))
     else:
         check(load().inscy_run_batch(ptrs, ns, ds, B, ctypes.byref(params), mode, outs))
     return [collect(outs[i]) for i in range(B)]
+
+
+# ---------------------------------------------------------------- cost model
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _mlp_check(rc):
+    if rc != 0:
+        raise InscyError(rc, load().inscy_mlp_last_error().decode())
+
+
+def mlp_nparams(n_in, hidden=64):
+    return int(load().inscy_mlp_params(n_in, hidden))
+
+
+def mlp_train(params, X, y, steps, lr):
+    """Full-batch Adam on the GPU; returns (new params, loss before each step)."""
+    params = np.array(params, dtype=np.float32, copy=True)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    hist = np.zeros(max(1, steps), np.float32)
+    _mlp_check(load().inscy_mlp_train(_fptr(params), X.shape[1], 64, _fptr(X), _fptr(y), X.shape[0], steps, lr,
+                                      _fptr(hist)))
+    return params, hist[:steps]
+
+
+def mlp_predict(params, X):
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    out = np.zeros(X.shape[0], np.float32)
+    _mlp_check(load().inscy_mlp_predict(_fptr(params), X.shape[1], 64, _fptr(X), X.shape[0], _fptr(out)))
+    return out
+
+
+def mlp_grad(params, X, y):
+    """(loss, gradient) of the mean squared error at params, computed on the GPU."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    grad = np.zeros_like(params)
+    loss = np.zeros(1, np.float32)
+    _mlp_check(load().inscy_mlp_grad(_fptr(params), X.shape[1], 64, _fptr(X), _fptr(y), X.shape[0], _fptr(grad),
+                                     _fptr(loss)))
+    return float(loss[0]), grad

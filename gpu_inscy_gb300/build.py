@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libinscy_gb300.so")
 SOURCES = ["engine.cu", "kernels_setup.cu", "kernels_density.cu", "kernels_tree.cu", "kernels_cluster.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-fmad=false",
          "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-Xptxas", "-v"]

@@ -116,6 +116,25 @@ int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, in
 int inscy_run_batch_scheduled(const float* const* Xs, const int64_t* ns, const int* ds, int count,
                               const inscy_params* p, const int* order, int lanes, inscy_result** outs);
 
+/* Cost model of the batch scheduler (no counterpart in the reference): an MLP
+ * in -> 64 -> 64 -> 1 with ReLU, parameters flat float32 in the order W1 (64 x
+ * in, row-major), b1 (64), W2 (64 x 64), b2 (64), w3 (64), b3 (1):
+ * inscy_mlp_params(in, 64) of them (-1 for a bad shape).  Rows of X are
+ * feature vectors, row-major [rows, in].  Training runs `steps` full-batch Adam
+ * steps (beta 0.9/0.999, eps 1e-8, learning rate lr) of the mean squared error
+ * on the GPU and updates `params` in place; loss_hist[t] receives the loss
+ * before step t.  inscy_mlp_grad returns the loss and its gradient at
+ * `params` (for checking the training kernels).  hidden must be 64 and
+ * 1 <= in <= 64.  These functions allocate device memory per call.  On error
+ * they return a nonzero code and inscy_mlp_last_error() describes it. */
+int inscy_mlp_params(int in, int hidden);
+int inscy_mlp_train(float* params, int in, int hidden, const float* X, const float* y, int rows, int steps, float lr,
+                    float* loss_hist);
+int inscy_mlp_predict(const float* params, int in, int hidden, const float* X, int rows, float* out);
+int inscy_mlp_grad(const float* params, int in, int hidden, const float* X, const float* y, int rows, float* grad,
+                   float* loss);
+const char* inscy_mlp_last_error(void);
+
 /* Result access. */
 int inscy_result_count(const inscy_result* r);              /* number of clustered subspaces */
 int64_t inscy_result_n(const inscy_result* r);              /* number of points */
