@@ -17,6 +17,10 @@ clustered per second (n / run time) and ms per run.
   cpu_baseline -- the CPU restatement of the reference CPU INSCY (oracle/) on a
              bounded sample of the workload, all host cores.
 
+batched -- the 64-dataset batch workload: plain runs one after another vs the
+             batched form (concurrent lanes) with FIFO and with the learned
+             schedule (cost model trained on the committed cost records).
+
 `--impl reference` times the reference's CPU INSCY path (the oracle port of
 run_cpu3_weak) instead.  Multi-GPU: replicas only (`--gpus N` under torchrun
 runs N independent copies of the workload, one per GPU).
@@ -50,6 +54,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2000, help="rows of the workload the CPU baseline runs on")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the label check against the oracle")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched / learned-schedule measurement")
     return ap.parse_args()
 
 
@@ -127,6 +132,58 @@ def cpu_baseline(X, p, sample_rows, steps=1):
     return {"value": Xs.shape[0] / t, "unit": "points/s", "cores": cores, "kind": "port",
             "sample": "first %d of the %d rows of the %s workload, same parameters; %.2f s per run"
                       % (Xs.shape[0], X.shape[0], WORKLOAD, t)}
+
+
+def batched_block(_lib):
+    """The batched form on the 64-dataset batch workload (seed 0, held out from
+    the cost records): plain (sequential) vs concurrent lanes with the FIFO
+    schedule vs the learned (longest predicted first) schedule; the lane
+    count is autotuned on a subset."""
+    from gpu_inscy_gb300 import scheduler, synth
+    Xs = synth.make_batch(0)
+    p = dict(synth.PARAMS["batch"])
+    params = _lib.make_params(**p)
+    points = int(sum(x.shape[0] for x in Xs))
+    plain, t_plain = [], []
+    for X in Xs:
+        t0 = time.perf_counter()
+        plain.append(_lib.run_host(X, params)[:2])
+        t_plain.append(time.perf_counter() - t0)
+    # cost model from the committed records (none of them from this batch)
+    recs = scheduler.load_records()
+    model = scheduler.CostModel(seed=0).fit([r["features"] for r in recs], [r["ms"] for r in recs])
+    F = np.array([scheduler.features(X, **p) for X in Xs])
+    pred = model.predict_ms(F)
+    err = float(np.median(np.abs(np.log(pred) - np.log(1000.0 * np.asarray(t_plain)))))
+    learned = scheduler.lpt_order(pred)
+    # autotune the lane count on the first 24 datasets
+    sub = Xs[:24]
+    tried = {}
+    for lanes in (2, 4, 8):
+        _lib.run_batch(sub, params, _lib.MODE_BATCHED, lanes=lanes)  # warm the lanes' engines
+        t0 = time.perf_counter()
+        _lib.run_batch(sub, params, _lib.MODE_BATCHED, lanes=lanes)
+        tried[lanes] = time.perf_counter() - t0
+    lanes = min(tried, key=tried.get)
+    _lib.run_batch(Xs, params, _lib.MODE_BATCHED, lanes=lanes)  # warm-up at the chosen lane count
+    t0 = time.perf_counter()
+    fifo = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, lanes=lanes)
+    t_fifo = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    lrn = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, order=learned, lanes=lanes)
+    t_learned = time.perf_counter() - t0
+    same = all(a[0] == b[0] and a[0] == c[0] and np.array_equal(np.asarray(a[1]), np.asarray(b[1])) and
+               np.array_equal(np.asarray(a[1]), np.asarray(c[1])) for a, b, c in zip(plain, fifo, lrn))
+    return {"workload": "batch64_seed0 (64 datasets, n log-uniform in [2000, 50000], d in [8, 20])",
+            "datasets": len(Xs), "points": points, "lanes": lanes,
+            "lanes_tried_s": {str(k): round(v, 3) for k, v in tried.items()},
+            "plain_s": round(sum(t_plain), 3), "fifo_s": round(t_fifo, 3), "learned_s": round(t_learned, 3),
+            "plain_points_per_s": points / sum(t_plain), "fifo_points_per_s": points / t_fifo,
+            "learned_points_per_s": points / t_learned,
+            "learned_vs_plain": sum(t_plain) / t_learned, "learned_vs_fifo": t_fifo / t_learned,
+            "cost_model": {"records": len(recs), "median_abs_log_error": err,
+                           "final_train_loss": float(model.loss_hist[-1])},
+            "labels_equal_plain": bool(same)}
 
 
 def run_reference(args, X, p):
@@ -247,6 +304,8 @@ def main():
             "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
             "commit_counters": st["replay"],
             "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_block(_lib)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(X, p, args.cpu_sample)
     if rank == 0:
