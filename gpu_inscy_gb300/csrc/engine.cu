@@ -406,9 +406,11 @@ struct HostParams {
   int num_obj, min_size, cells, rect;
 };
 
-// host-pool workers of engines created on this thread (-1: by the core count;
-// batch lanes set it so that concurrent engines share the cores)
+// host-pool workers of engines created on this thread (-1: by the core count)
+// and the single-pass list budget of their runs: batch lanes divide both
+// among the concurrent engines
 thread_local int t_pool_workers = -1;
+thread_local long long t_single_pass_bytes = kSinglePassBytes;
 
 // ---------------------------------------------------------------------------
 // the engine (one run at a time; device resources are kept between runs)
@@ -899,7 +901,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         launch_exclusive_scan_ll(cap, cbase, ngroup_warps, dtot, sums, s);
         launches += 4;
         const long long capt = scalar(dtot, s);
-        if (capt * 8 <= kSinglePassBytes) {
+        if (capt * 8 <= t_single_pass_bytes) {
           single = true;
           L = capt;
           lids = keepmem->get<int>(L);
@@ -1905,7 +1907,8 @@ int run_common(const float* X, bool on_device, int64_t n, int d, const inscy_par
 // run at once -- their kernels overlap on the GPU and their commits on the
 // host cores.  A lane takes the next dataset of the schedule when its last
 // one is done.  The lanes stay parked between calls (engines keep their
-// warmed pools); a call with another device or lane count makes a new set.
+// warmed pools); a call with another device or lane count replaces the set
+// (the old lanes exit and free their engines).
 struct BatchJob {
   const float* X;
   int64_t n;
@@ -1919,7 +1922,16 @@ class LanePool {
  public:
   LanePool(int device, int lanes) : device_(device), lanes_(lanes) {
     for (int i = 0; i < lanes; ++i) th_.emplace_back([this] { lane_main(); });
-    for (auto& t : th_) t.detach();  // parked until exit
+  }
+  // the lanes exit; their engines (memory pools, streams) go with them
+  ~LanePool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
   }
   int device() const { return device_; }
   int lanes() const { return lanes_; }
@@ -1940,6 +1952,7 @@ class LanePool {
     cudaSetDevice(device_);
     const int hw = (int)std::thread::hardware_concurrency();
     inscy::t_pool_workers = std::max(0, std::min(7, hw / (2 * lanes_) - 1));
+    inscy::t_single_pass_bytes = inscy::kSinglePassBytes / lanes_;
     cudaStream_t s = nullptr;
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     long long seen = 0;
@@ -1950,6 +1963,7 @@ class LanePool {
         std::unique_lock<std::mutex> lk(m_);
         cv_.wait(lk, [&] { return gen_ != seen; });
         seen = gen_;
+        if (stop_) break;
         jobs = jobs_;
         p = p_;
       }
@@ -1963,8 +1977,11 @@ class LanePool {
       std::lock_guard<std::mutex> lk(m_);
       if (--active_ == 0) done_.notify_all();
     }
+    g_engine.reset();
+    cudaStreamDestroy(s);
   }
   int device_, lanes_;
+  bool stop_ = false;
   std::vector<std::thread> th_;
   std::mutex m_;
   std::condition_variable cv_, done_;
@@ -1976,7 +1993,7 @@ class LanePool {
 };
 
 std::mutex g_lanes_m;
-LanePool* g_lanes = nullptr;  // the current lane set (earlier sets stay parked)
+LanePool* g_lanes = nullptr;  // the current lane set (not torn down at exit)
 
 constexpr int kDefaultLanes = 4;
 }  // namespace
@@ -2012,7 +2029,11 @@ int inscy_run_batch_scheduled(const float* const* Xs, const int64_t* ns, const i
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(INSCY_ERR_CUDA, "cudaGetDevice failed");
   {
     std::lock_guard<std::mutex> g(g_lanes_m);  // one scheduled batch at a time per process
-    if (!g_lanes || g_lanes->device() != dev || g_lanes->lanes() != lanes) g_lanes = new LanePool(dev, lanes);
+    if (!g_lanes || g_lanes->device() != dev || g_lanes->lanes() != lanes) {
+      delete g_lanes;
+      g_lanes = nullptr;
+      g_lanes = new LanePool(dev, lanes);
+    }
     g_lanes->run(jobs, p);
   }
   for (const BatchJob& j : jobs)
