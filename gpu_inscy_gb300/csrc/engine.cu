@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -70,6 +71,12 @@ const double kPi = 3.14;  // ClusteringCpu.cu:27
 #define INSCY_SINGLE_PASS_BYTES (32LL << 30)
 #endif
 constexpr long long kSinglePassBytes = INSCY_SINGLE_PASS_BYTES;
+// density pass over point rows (k_neighbours_rows) when d <= kRowSlots; 0
+// keeps the general kernel for every d (both give the same lists)
+#ifndef INSCY_DENSITY_ROWS
+#define INSCY_DENSITY_ROWS 1
+#endif
+constexpr bool kDensityRows = INSCY_DENSITY_ROWS != 0;
 // narrowest leaf key the level kernel may use (4; raised only to test the wider forms)
 #ifndef INSCY_TREE_MIN_KEY_BYTES
 #define INSCY_TREE_MIN_KEY_BYTES 4
@@ -626,6 +633,43 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   };
   launch_prep(dX, ni, d, cells, csz, G, fsz, hp.eps, dcc, dfc, dgz, s);
   ++launches;
+  // point rows for the density pass when a row fits kRowSlots slots
+  float* dxrow = nullptr;
+  float* dwin = nullptr;
+  unsigned long long* dwork = persist.get<unsigned long long>(1);
+  if (kDensityRows && d <= kRowSlots) {
+    // fine_lo[k]: the least float x in [0, 1] whose fine cell before the cap,
+    // (int)(x / fsz), is >= k (+inf if none); the cell is monotone in x, so
+    // the +-1 fine-cell test becomes an interval test on the coordinate
+    std::vector<float> fine_lo(G + 2);
+    for (int k = 0; k <= G + 1; ++k) {
+      auto reaches = [&](uint32_t b) {
+        float x;
+        std::memcpy(&x, &b, 4);
+        return (int)(x / fsz) >= k;
+      };
+      const uint32_t one = 0x3f800000u;  // 1.0f: inputs lie in [0, 1]
+      if (!reaches(one)) {
+        fine_lo[k] = std::numeric_limits<float>::infinity();
+        continue;
+      }
+      uint32_t lo = 0, hi = one;  // least b in [lo, hi] that reaches k
+      while (lo < hi) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        if (reaches(mid))
+          hi = mid;
+        else
+          lo = mid + 1;
+      }
+      std::memcpy(&fine_lo[k], &lo, 4);
+    }
+    float* dfine = persist.get<float>(G + 2);
+    h2d(dfine, fine_lo.data(), sizeof(float) * (G + 2), s);
+    dxrow = persist.get<float>((size_t)n * kRowSlots);
+    dwin = persist.get<float>((size_t)n * kRowSlots * 2);
+    launch_point_rows(dX, dfc, ni, d, G, dfine, dxrow, dwin, s);
+    ++launches;
+  }
   int* drank = persist.get<int>(n);
   int* dbucket = persist.get<int>((size_t)n * d);
   int* dboff = persist.get<int>((size_t)d * (G + 1));
@@ -862,11 +906,17 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.out_counter = dcand_cnt + 2;
       DL.cap_base = nullptr;
       DL.cap_loff = nullptr;
+      DL.xrow = dxrow;
+      DL.win = dwin;
+      DL.work = dxrow ? dwork : nullptr;
+      DL.items = nullptr;
       auto neighbours = [&](bool write) {
-        if (level == 1)
+        if (level == 1) {
           launch_neighbours(DL, write, s);
-        else
+        } else {
+          if (DL.work) CK(cudaMemsetAsync(DL.work, 0, sizeof(unsigned long long), s));
           launch_neighbours_multi(DL, ngroup_warps, write, s);
+        }
       };
       // algorithmic bytes of the candidate pass: per (subspace, point) 26 B (its
       // id, list offset and length, own coordinate and fine cell, count out);
@@ -897,6 +947,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       if (level > 1) {
         long long* cap = lv.get<long long>(ngroup_warps + 1);
         long long* cbase = lv.get<long long>(ngroup_warps + 1);
+        if (DL.work) DL.items = lv.get<RowItem>(ngroup_warps);  // the row kernel's pair records
         launch_list_capacity(DL, ngroup_warps, cap, s);
         launch_exclusive_scan_ll(cap, cbase, ngroup_warps, dtot, sums, s);
         launches += 4;

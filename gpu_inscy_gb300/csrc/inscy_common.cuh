@@ -14,6 +14,7 @@
 //   * region       -- one restriction of a call to (dim, run of cells), after
 //                     mergeWithNeighbors (ScyTreeNode.cu:837-851).
 #pragma once
+#include <cstring>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -22,6 +23,7 @@ namespace inscy {
 constexpr int kMaxDims = 64;    // subspaces are 64-bit masks
 constexpr int kMaxCells = 255;  // coarse cells fit a byte
 constexpr int kWarp = 32;
+constexpr int kRowSlots = 16;   // point rows of the density pass (d <= 16)
 
 // Region record written by the level kernel (one per restriction run).
 struct RegionRec {
@@ -72,6 +74,21 @@ struct GroupDesc {
   int pad;
 };
 
+// One (group, query) pair of a level >= 2 density pass, resolved once by the
+// capacity kernel for the row kernel: the query point, its parent list, and
+// the group's children (dims d0 .. d0 + nc - 1, subspaces sub_base ..).
+// len < 0 marks a pair whose checks failed (the guard holds the reason).
+struct alignas(16) RowItem {
+  long long pb;  // parent-list start
+  int len;       // parent-list length
+  int p;         // query point
+  int sub_base;  // first child subspace
+  int i;         // query index within the group
+  short d0;      // first child's dim
+  short nc;      // children
+  int pad;
+};
+
 // Device-side consistency checks: the first failed check records its code and
 // the offending value; the caller skips the access and the host reports the
 // failure after the launch (INSCY_ERR_INTERNAL) instead of touching memory out
@@ -95,6 +112,27 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
+
+// Asynchronous 16-byte global -> shared copies of one thread (cp.async, cached
+// in L1): both addresses 16-byte aligned; a thread's copies complete in the
+// order of its commit groups, and async_wait<N> waits until at most N of its
+// groups are pending.  Host execution of these sources copies at once.
+#ifdef __CUDACC__
+__device__ __forceinline__ void async_copy16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+#else
+inline void async_copy16(void* smem, const void* gmem) { std::memcpy(smem, gmem, 16); }
+inline void async_commit() {}
+template <int N>
+inline void async_wait() {}
+#endif
 
 // Squared-distance step of dist() (ClusteringCpu.cu:40-50): acc + diff*diff
 // with each operation rounded separately (no fused multiply-add).

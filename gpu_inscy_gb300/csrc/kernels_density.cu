@@ -69,6 +69,12 @@ struct DensityArgs {
   // its length; the kernel writes every item's count and list start (cap_loff)
   const long long* cap_base;
   long long* cap_loff;
+  // point rows (d <= kRowSlots) and the work counter of k_neighbours_rows
+  const float* xrow;
+  const float* win;
+  unsigned long long* work;
+  RowItem* items;        // per (group, query): written by k_list_capacity, read by k_neighbours_rows
+  int chunk;             // (group, query) pairs a warp takes per counter update
   long long prev_total;  // entries in the previous level's lists
   long long total;       // entries in this level's lists (write passes)
   long long prev_nkeep;  // kept points of the previous level
@@ -106,8 +112,35 @@ __device__ __forceinline__ void locate(const DensityArgs& a, long long w, int& s
 
 // count (kWrite = false) or write (kWrite = true) the ordered neighbour list
 // of one (subspace, point): candidates 32 at a time, accepted lanes by ballot
+// Per-block sums of the statistics counters: one shared add per warp and one
+// global add per block (per-warp global atomics on the same few counters
+// saturate the L2 slice that holds them).
+struct BlockStats {
+  unsigned long long cand, list;
+};
+__device__ __forceinline__ void block_stats_begin(BlockStats& s) {
+  if (threadIdx.x == 0) s.cand = s.list = 0;
+  __syncthreads();
+}
+__device__ __forceinline__ void block_stats_end(BlockStats& s, const DensityArgs& a, unsigned long long cand,
+                                                unsigned long long list) {
+  if (lane_id() == 0 && (cand || list)) {
+    atomicAdd(&s.cand, cand);
+    atomicAdd(&s.list, list);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (a.cand_counter && s.cand) atomicAdd(a.cand_counter, s.cand);
+    if (a.list_counter && s.list) atomicAdd(a.list_counter, s.list);
+  }
+}
+
 template <bool kWrite>
 __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
+  __shared__ BlockStats bs;
+  if (!kWrite) block_stats_begin(bs);
+  unsigned long long n_len = 0;  // the warp's list length (count pass)
+  [&] {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= a.nwarps) return;
   const unsigned lane = lane_id();
@@ -165,11 +198,10 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     }
     count += __popc(m);
   }
-  if (!kWrite && lane == 0) {
-    a.cnt[item] = count;
-    if (a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len);
-    if (a.list_counter) atomicAdd(a.list_counter, (unsigned long long)len);
-  }
+  if (!kWrite && lane == 0) a.cnt[item] = count;
+  n_len = (unsigned long long)len;
+  }();
+  if (!kWrite) block_stats_end(bs, a, n_len, n_len);
 }
 
 // Levels >= 2: every child subspace of a parent filters the same parent list
@@ -178,7 +210,17 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
 // cells is loaded once).  Lane c keeps the running count of child c (and
 // c + 32).
 template <bool kWrite>
-__global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
+__global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
+  const bool single = kWrite && a.cap_base != nullptr;
+  const bool stats = !kWrite || single;
+  __shared__ BlockStats bs;
+  __shared__ unsigned long long bs_out;
+  if (stats) {
+    if (threadIdx.x == 0) bs_out = 0;
+    block_stats_begin(bs);
+  }
+  unsigned long long n_cand = 0, n_list = 0;
+  [&] {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= a.nwarps) return;
   const unsigned lane = lane_id();
@@ -207,7 +249,6 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
   const uint8_t* frow_p = a.fc + (size_t)p * a.d;
   int run0 = 0, run1 = 0;  // lane c: children c and c + 32
   long long ob0 = 0, ob1 = 0;
-  const bool single = kWrite && a.cap_base != nullptr;
   if (single) {
     ob0 = a.cap_base[w] + (long long)lane * len;
     ob1 = a.cap_base[w] + (long long)(lane + 32) * len;
@@ -219,11 +260,12 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
     const long long j = j0 + lane;
     bool in = j < len;
     int q = in ? ids[j] : p;
+    const float acc0 = in ? accs[j] : 0.f;  // loaded before the id check, which may store
     if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
       in = false;
       q = p;
     }
-    const float acc = in ? accs[j] : 0.f;
+    const float acc = in ? acc0 : 0.f;
     const float* xrow_q = a.X + (size_t)q * a.d;
     const uint8_t* frow_q = a.fc + (size_t)q * a.d;
     for (int c = 0; c < nc; ++c) {
@@ -268,18 +310,193 @@ __global__ void __launch_bounds__(256) k_neighbours_multi(DensityArgs a) {
       a.cnt[item] = run1;
       if (single) a.cap_loff[item] = ob1;
     }
-    if (lane == 0 && a.cand_counter) atomicAdd(a.cand_counter, (unsigned long long)len * nc);
-    if (lane == 0 && a.list_counter) atomicAdd(a.list_counter, (unsigned long long)len);
+    n_cand = (unsigned long long)len * nc;
+    n_list = (unsigned long long)len;
     if (single && a.out_counter) {
       int tot = ((int)lane < nc ? run0 : 0) + ((int)lane + 32 < nc ? run1 : 0);
       for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-      if (lane == 0) atomicAdd(a.out_counter, (unsigned long long)tot);
+      if (lane == 0 && tot) atomicAdd(&bs_out, (unsigned long long)tot);
+    }
+  }
+  }();
+  if (stats) {
+    block_stats_end(bs, a, n_cand, n_list);  // its barrier also orders the adds to bs_out
+    if (threadIdx.x == 0 && single && a.out_counter && bs_out) atomicAdd(a.out_counter, bs_out);
+  }
+}
+
+// Levels >= 2 when d <= kRowSlots: the same tests and outputs as
+// k_neighbours_multi, with
+//   * the (group, query) pair read from its record (RowItem, resolved by
+//     k_list_capacity), so a pair starts after one load instead of a search
+//     and a chain of dependent loads;
+//   * every candidate's row of coordinates (16 floats, 64 bytes; the 16-byte
+//     quarters below the first child's dim are skipped) fetched once, and the
+//     children walked by a loop over the 16 dims unrolled at compile time (a
+//     group's children extend the parent by the consecutive dims d0 .. d0 +
+//     nc - 1, child c = dim d0 + c), so a (candidate, child) test reads
+//     registers only.  The +-1 fine-cell test is the equivalent interval test
+//     lo_p <= x_q < hi_p on the query's precomputed window, so no fine cell
+//     of the candidate is read;
+//   * a software pipeline over the 32-candidate chunks of a list: the ids and
+//     partial distances of chunk k + 2 are loaded into registers and the rows
+//     of chunk k + 1 are copied to shared memory (cp.async, one 64-byte slot
+//     per lane, two buffers) while chunk k is tested;
+//   * the query's coordinates and windows copied the same way into a per-warp
+//     slot (warp-uniform reads);
+//   * warps taking `chunk` (group, query) pairs at a time from a work counter,
+//     so a warp whose list was short takes the next pair instead of idling
+//     until the longest list of its block is done.
+constexpr int kRowsBlocksPerSM = 4;
+constexpr int kRowsSMs = 152;
+constexpr int kRowBytes = kRowSlots * 4;  // 16 coordinates
+
+struct RowsShared {
+  alignas(16) float qx[8][kRowSlots];                   // the query's coordinates, per warp
+  alignas(16) float qwin[8][kRowSlots][2];              // ... and its fine-cell windows [lo, hi)
+  alignas(16) unsigned char rows[8][2][32][kRowBytes];  // per warp, two buffers, one slot per lane
+};
+
+template <bool kWrite>
+__global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(DensityArgs a) {
+  __shared__ RowsShared sh;
+  const unsigned lane = lane_id();
+  const int wb = (int)(threadIdx.x >> 5);
+  const bool single = kWrite && a.cap_base != nullptr;
+  unsigned char* slot0 = sh.rows[wb][0][lane];
+  unsigned char* slot1 = sh.rows[wb][1][lane];
+  const float* qx = sh.qx[wb];
+  const float(*qwin)[2] = sh.qwin[wb];
+  // the warp's statistics, added to the global counters once when it exits
+  // (per-pair atomics on three adjacent counters saturate one L2 slice)
+  unsigned long long n_cand = 0, n_list = 0, n_out = 0;
+  for (;;) {
+    unsigned long long take = 0;
+    if (lane == 0) take = atomicAdd(a.work, (unsigned long long)a.chunk);
+    const long long w0 = (long long)__shfl_sync(0xffffffffu, take, 0);
+    if (w0 >= a.nwarps) break;
+    const long long w1 = w0 + a.chunk < a.nwarps ? w0 + a.chunk : a.nwarps;
+    for (long long w = w0; w < w1; ++w) {
+      const RowItem r = a.items[w];
+      if (r.len < 0) continue;  // failed its checks (reported by the capacity kernel)
+      const int p = r.p, nc = r.nc, D0 = r.d0;
+      const long long len = r.len;
+      const int* ids = a.prev_lids + r.pb;
+      const float* accs = a.prev_lacc + r.pb;
+      // lane c: the work item of child c (read now, used after the list)
+      const long long item_c = (int)lane < nc ? a.subs[r.sub_base + lane].item_off + r.i : 0;
+      int run = 0;  // lane c: entries of child c so far
+      long long ob = 0;
+      if (single) {
+        ob = a.cap_base[w] + (long long)lane * len;
+      } else if (kWrite) {
+        if ((int)lane < nc) ob = a.loff[item_c];
+      }
+      // candidate j of the list (lanes past the end stand on the query
+      // itself); nothing reads the loaded values until copy_row, a chunk later
+      auto fetch = [&](long long j, bool& in, int& q, float& acc) {
+        in = j < len;
+        q = in ? ids[j] : p;
+        acc = in ? accs[j] : 0.f;
+      };
+      // the id is checked where it is first used: the copy of its row
+      auto copy_row = [&](unsigned char* slot, bool& in, int& q) {
+        if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
+          in = false;
+          q = p;
+        }
+        const unsigned char* xr = reinterpret_cast<const unsigned char*>(a.xrow + (size_t)q * kRowSlots);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (4 * t + 3 >= D0) async_copy16(slot + 16 * t, xr + 16 * t);  // quarters below d0 are not read
+      };
+      const long long nchunks = (len + 31) >> 5;
+      bool in_a = false, in_b = false;
+      int q_a = p, q_b = p;
+      float acc_a = 0.f, acc_b = 0.f;
+      __syncwarp();  // the previous pair's reads of the query slot are done
+      if (lane < 12) {  // 4 x 16 B of coordinates, 8 x 16 B of windows
+        if (lane < 4)
+          async_copy16(reinterpret_cast<unsigned char*>(sh.qx[wb]) + 16 * lane,
+                       reinterpret_cast<const unsigned char*>(a.xrow + (size_t)p * kRowSlots) + 16 * lane);
+        else
+          async_copy16(reinterpret_cast<unsigned char*>(sh.qwin[wb]) + 16 * (lane - 4),
+                       reinterpret_cast<const unsigned char*>(a.win + (size_t)p * kRowSlots * 2) + 16 * (lane - 4));
+      }
+      async_commit();  // group: the query row
+      if (nchunks > 0) {
+        fetch(lane, in_a, q_a, acc_a);
+        copy_row(slot0, in_a, q_a);
+      }
+      async_commit();  // group: the rows of chunk 0
+      if (nchunks > 1) fetch(32 + lane, in_b, q_b, acc_b);
+      async_wait<1>();  // the query row has landed
+      __syncwarp();     // ... and is visible to the whole warp
+      for (long long k = 0; k < nchunks; ++k) {
+        // chunk k + 1: rows in flight; chunk k + 2: ids and distances in flight
+        if (k + 1 < nchunks) copy_row((k & 1) ? slot0 : slot1, in_b, q_b);
+        async_commit();
+        const bool in = in_a;
+        const int q = q_a;
+        const float acc = acc_a;
+        in_a = in_b;
+        q_a = q_b;
+        acc_a = acc_b;
+        if (k + 2 < nchunks) fetch(((k + 2) << 5) + lane, in_b, q_b, acc_b);
+        async_wait<1>();  // this lane's copy of chunk k is in its slot
+        const unsigned char* slot = (k & 1) ? slot1 : slot0;
+        const float4 x0 = *reinterpret_cast<const float4*>(slot);
+        const float4 x1 = *reinterpret_cast<const float4*>(slot + 16);
+        const float4 x2 = *reinterpret_cast<const float4*>(slot + 32);
+        const float4 x3 = *reinterpret_cast<const float4*>(slot + 48);
+        const float xq[kRowSlots] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
+                                     x2.x, x2.y, x2.z, x2.w, x3.x, x3.y, x3.z, x3.w};
+        const bool live = in && q != p;
+#pragma unroll
+        for (int D = 0; D < kRowSlots; ++D) {
+          const int c = D - D0;
+          if (c < 0 || c >= nc) continue;  // warp-uniform
+          const float acc2 = dist_step(acc, qx[D], xq[D]);
+          const bool ok = live && xq[D] >= qwin[D][0] && xq[D] < qwin[D][1] && acc2 <= a.acc_max;
+          const unsigned m = __ballot_sync(0xffffffffu, ok);
+          if (!m) continue;
+          if (kWrite) {
+            const long long base = __shfl_sync(0xffffffffu, ob + run, c);
+            if (ok) {
+              const long long o = base + __popc(m & lanemask_lt());
+              if (GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) {
+                a.lids[o] = q;
+                a.lacc[o] = acc2;
+              }
+            }
+          }
+          if ((int)lane == c) run += __popc(m);
+        }
+      }
+      if (!kWrite || single) {
+        if ((int)lane < nc) {
+          a.cnt[item_c] = run;
+          if (single) a.cap_loff[item_c] = ob;
+          n_out += (unsigned long long)run;
+        }
+        n_cand += (unsigned long long)len * nc;
+        n_list += (unsigned long long)len;
+      }
+    }
+  }
+  if (!kWrite || single) {
+    for (int o = 16; o > 0; o >>= 1) n_out += __shfl_xor_sync(0xffffffffu, n_out, o);
+    if (lane == 0) {
+      if (a.cand_counter) atomicAdd(a.cand_counter, n_cand);
+      if (a.list_counter) atomicAdd(a.list_counter, n_list);
+      if (single && a.out_counter) atomicAdd(a.out_counter, n_out);
     }
   }
 }
 
 // single-pass list capacity of every (group, query): children x the query's
-// parent-list length
+// parent-list length; with `a.items`, also the pair's record for the row
+// kernel (query point, parent list, children), checked here once
 __global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= a.nwarps) return;
@@ -295,8 +512,34 @@ __global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
   const long long i = w - g.qwarp_off;
   const long long k = a.subs[g.sub_base].query_off + i;
   long long len = 0;
-  if (GUARD_OK(a.guard, i >= 0 && i < g.nquery && k < a.prev_nkeep, 36, k)) len = a.prev_lcnt[k];
+  const bool ok = GUARD_OK(a.guard, i >= 0 && i < g.nquery && k < a.prev_nkeep, 36, k);
+  if (ok) len = a.prev_lcnt[k];
   cap[w] = (long long)g.nchild * len;
+  if (!a.items) return;
+  RowItem r;
+  r.pb = 0;
+  r.len = -1;
+  r.p = 0;
+  r.sub_base = g.sub_base;
+  r.i = (int)i;
+  r.d0 = (short)a.subs[g.sub_base].dim;
+  r.nc = (short)g.nchild;
+  r.pad = 0;
+  if (ok) {
+    const int p = a.prev_keep[k];
+    const long long pb = a.prev_loff[k];
+    const int nc = g.nchild, d0 = a.subs[g.sub_base].dim;
+    if (GUARD_OK(a.guard,
+                 d0 >= 0 && nc >= 1 && d0 + nc <= kRowSlots && a.subs[g.sub_base + nc - 1].dim == d0 + nc - 1, 37,
+                 d0) &&
+        GUARD_OK(a.guard, p >= 0 && p < a.n, 32, p) &&
+        GUARD_OK(a.guard, pb >= 0 && len >= 0 && pb + len <= a.prev_total, 33, pb + len)) {
+      r.pb = pb;
+      r.len = (int)len;
+      r.p = p;
+    }
+  }
+  a.items[w] = r;
 }
 
 // density of every (subspace, point) from its list.  The phi sum of one item
@@ -491,6 +734,11 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.out_counter = L.out_counter;
   a.cap_base = L.cap_base;
   a.cap_loff = L.cap_loff;
+  a.xrow = L.xrow;
+  a.win = L.win;
+  a.work = L.work;
+  a.items = L.items;
+  a.chunk = 1;
   a.prev_total = L.prev_total;
   a.total = L.total;
   a.prev_nkeep = L.prev_nkeep;
@@ -547,6 +795,20 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
   if (nwarps <= 0) return;
   DensityArgs a = make_args(L);
   a.nwarps = nwarps;
+  if (L.xrow && L.win && L.work && L.items && L.d <= kRowSlots) {
+    // persistent warps: a grid that fills every SM once, (group, query) pairs
+    // handed out by the work counter, several per update when there are many
+    const long long resident = (long long)kRowsSMs * kRowsBlocksPerSM * 8;
+    long long chunk = nwarps / (resident * 16);
+    a.chunk = (int)(chunk < 1 ? 1 : chunk > 8 ? 8 : chunk);
+    const long long need = (nwarps + 7) / 8;
+    const unsigned blocks = (unsigned)(need < kRowsSMs * kRowsBlocksPerSM ? need : kRowsSMs * kRowsBlocksPerSM);
+    if (write)
+      k_neighbours_rows<true><<<blocks, 256, 0, s>>>(a);
+    else
+      k_neighbours_rows<false><<<blocks, 256, 0, s>>>(a);
+    return;
+  }
   unsigned blocks = (unsigned)((nwarps * 32 + 255) / 256);
   if (write)
     k_neighbours_multi<true><<<blocks, 256, 0, s>>>(a);

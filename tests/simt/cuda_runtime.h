@@ -29,6 +29,12 @@ struct dim3 {
 struct int2 {
   int x, y;
 };
+struct alignas(16) float4 {
+  float x, y, z, w;
+};
+struct alignas(16) uint4 {
+  unsigned x, y, z, w;
+};
 inline int2 make_int2(int a, int b) { return int2{a, b}; }
 using std::max;
 using std::min;
@@ -79,6 +85,7 @@ inline T __shfl_xor_sync(unsigned m, T v, int o) {
 }
 inline unsigned __ballot_sync(unsigned m, int p) { return (unsigned)simt::collective(simt::OP_BALLOT, m, p ? 1 : 0, 0); }
 inline int __any_sync(unsigned m, int p) { return (int)simt::collective(simt::OP_ANY, m, p ? 1 : 0, 0); }
+inline void __syncwarp(unsigned m = 0xffffffffu) { (void)simt::collective(simt::OP_ANY, m, 0, 0); }
 template <class T>
 inline unsigned __match_any_sync(unsigned m, T v) {
   return (unsigned)simt::collective(simt::OP_MATCH_ANY, m, simt::to_bits(v), (int)sizeof(T));
@@ -176,6 +183,10 @@ cudaError_t cudaMemcpy(void* d, const void* s, size_t n, cudaMemcpyKind k);
 cudaError_t cudaMemsetAsync(void* d, int v, size_t n, cudaStream_t st = 0);
 cudaError_t cudaMemset(void* d, int v, size_t n);
 cudaError_t cudaStreamSynchronize(cudaStream_t s);
+enum { cudaStreamNonBlocking = 1 };
+cudaError_t cudaSetDevice(int d);
+cudaError_t cudaStreamCreateWithFlags(cudaStream_t* s, unsigned flags);
+cudaError_t cudaStreamDestroy(cudaStream_t s);
 cudaError_t cudaEventCreate(cudaEvent_t* e);
 cudaError_t cudaEventDestroy(cudaEvent_t e);
 cudaError_t cudaEventRecord(cudaEvent_t e, cudaStream_t s = 0);

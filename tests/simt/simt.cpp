@@ -442,6 +442,17 @@ cudaError_t cudaMemset(void* d, int v, size_t n) {
   return cudaSuccess;
 }
 cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
+// one device, and every launch runs to completion on the calling thread: a
+// stream is only a distinct handle
+cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+cudaError_t cudaStreamCreateWithFlags(cudaStream_t* s, unsigned) {
+  *s = (cudaStream_t) new char[1];
+  return cudaSuccess;
+}
+cudaError_t cudaStreamDestroy(cudaStream_t s) {
+  delete[] (char*)s;
+  return cudaSuccess;
+}
 cudaError_t cudaEventCreate(cudaEvent_t* e) {
   *e = (cudaEvent_t)0x1;
   return cudaSuccess;

@@ -82,7 +82,8 @@ def driver_big_blocks():
 @pytest.fixture(scope="module")
 def driver_key64():
     import build_simt
-    return build_simt.build(defines=("INSCY_TREE_MIN_KEY_BYTES=8",), tag="_key64")
+    # also keeps the general density kernel (no point rows) for d <= 16
+    return build_simt.build(defines=("INSCY_TREE_MIN_KEY_BYTES=8", "INSCY_DENSITY_ROWS=0"), tag="_key64")
 
 
 @pytest.fixture(scope="module")
@@ -107,6 +108,6 @@ def test_large_blocks_two_pass_lists_wide_keys(driver_big_blocks, plain_case, re
     assert_same(simt_run(driver_big_blocks, X, p, reverse, "small_big"), want, "small, 1024-thread items")
 
 
-def test_64_bit_leaf_keys(driver_key64, plain_case):
+def test_64_bit_leaf_keys_general_density_kernel(driver_key64, plain_case):
     X, p, want = plain_case
-    assert_same(simt_run(driver_key64, X, p, True, "plain_key64"), want, "plain n=1000, 64-bit keys")
+    assert_same(simt_run(driver_key64, X, p, True, "plain_key64"), want, "plain n=1000, 64-bit keys, no rows")
