@@ -331,45 +331,36 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 //     k_list_capacity), so a pair starts after one load instead of a search
 //     and a chain of dependent loads;
 //   * every candidate's row of coordinates (16 floats, 64 bytes; the 16-byte
-//     quarters below the first child's dim are skipped) fetched once, and the
-//     children walked by a loop over the 16 dims unrolled at compile time (a
-//     group's children extend the parent by the consecutive dims d0 .. d0 +
-//     nc - 1, child c = dim d0 + c), so a (candidate, child) test reads
-//     registers only.  The +-1 fine-cell test is the equivalent interval test
-//     lo_p <= x_q < hi_p on the query's precomputed window, so no fine cell
-//     of the candidate is read;
+//     quarters below the first child's dim are skipped) loaded once into
+//     registers, and the children walked by a loop over the 16 dims unrolled
+//     at compile time (a group's children extend the parent by the
+//     consecutive dims d0 .. d0 + nc - 1, child c = dim d0 + c), so a
+//     (candidate, child) test reads registers and one warp-uniform 16-byte
+//     shared load (the query's coordinate and fine-cell window on that dim).
+//     The +-1 fine-cell test is the equivalent interval test
+//     lo_p <= x_q < hi_p, so no fine cell of the candidate is read;
 //   * a software pipeline over the 32-candidate chunks of a list: the ids and
-//     partial distances of chunk k + 2 are loaded into registers and the rows
-//     of chunk k + 1 are copied to shared memory (cp.async, one 64-byte slot
-//     per lane, two buffers) while chunk k is tested;
-//   * the query's coordinates and windows copied the same way into a per-warp
-//     slot (warp-uniform reads);
+//     partial distances of chunk k + 2 and the rows of chunk k + 1 are loaded
+//     while chunk k is tested;
 //   * warps taking `chunk` (group, query) pairs at a time from a work counter,
 //     so a warp whose list was short takes the next pair instead of idling
 //     until the longest list of its block is done.
 constexpr int kRowsBlocksPerSM = 4;
 constexpr int kRowsSMs = 152;
-constexpr int kRowBytes = kRowSlots * 4;  // 16 coordinates
-
-struct RowsShared {
-  alignas(16) float qx[8][kRowSlots];                   // the query's coordinates, per warp
-  alignas(16) float qwin[8][kRowSlots][2];              // ... and its fine-cell windows [lo, hi)
-  alignas(16) unsigned char rows[8][2][32][kRowBytes];  // per warp, two buffers, one slot per lane
-};
 
 template <bool kWrite>
 __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(DensityArgs a) {
-  __shared__ RowsShared sh;
+  __shared__ float4 squery[8][kRowSlots];  // per warp and dim: the query's (x, lo, hi, -)
+  // per warp: candidate tests, list entries read, entries written; added to
+  // the global counters once when the warp exits (per-pair atomics on three
+  // adjacent counters saturate one L2 slice)
+  __shared__ unsigned long long sstat[8][3];
   const unsigned lane = lane_id();
   const int wb = (int)(threadIdx.x >> 5);
   const bool single = kWrite && a.cap_base != nullptr;
-  unsigned char* slot0 = sh.rows[wb][0][lane];
-  unsigned char* slot1 = sh.rows[wb][1][lane];
-  const float* qx = sh.qx[wb];
-  const float(*qwin)[2] = sh.qwin[wb];
-  // the warp's statistics, added to the global counters once when it exits
-  // (per-pair atomics on three adjacent counters saturate one L2 slice)
-  unsigned long long n_cand = 0, n_list = 0, n_out = 0;
+  const float4* xrow4 = reinterpret_cast<const float4*>(a.xrow);
+  const float4* qv = squery[wb];
+  if (lane == 0) sstat[wb][0] = sstat[wb][1] = sstat[wb][2] = 0;  // lane 0 alone touches them
   for (;;) {
     unsigned long long take = 0;
     if (lane == 0) take = atomicAdd(a.work, (unsigned long long)a.chunk);
@@ -392,50 +383,44 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
       } else if (kWrite) {
         if ((int)lane < nc) ob = a.loff[item_c];
       }
+      __syncwarp();  // the previous pair's reads of the query slot are done
+      if (lane < (unsigned)kRowSlots) {
+        const size_t t = (size_t)p * kRowSlots + lane;
+        squery[wb][lane] = make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
+      }
       // candidate j of the list (lanes past the end stand on the query
-      // itself); nothing reads the loaded values until copy_row, a chunk later
+      // itself); nothing reads the loaded values until load_row, a chunk later
       auto fetch = [&](long long j, bool& in, int& q, float& acc) {
         in = j < len;
         q = in ? ids[j] : p;
         acc = in ? accs[j] : 0.f;
       };
-      // the id is checked where it is first used: the copy of its row
-      auto copy_row = [&](unsigned char* slot, bool& in, int& q) {
+      // the id is checked where it is first used: the load of its row
+      auto load_row = [&](float4 (&x)[4], bool& in, int& q) {
         if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
           in = false;
           q = p;
         }
-        const unsigned char* xr = reinterpret_cast<const unsigned char*>(a.xrow + (size_t)q * kRowSlots);
 #pragma unroll
         for (int t = 0; t < 4; ++t)
-          if (4 * t + 3 >= D0) async_copy16(slot + 16 * t, xr + 16 * t);  // quarters below d0 are not read
+          if (4 * t + 3 >= D0) x[t] = xrow4[(size_t)q * 4 + t];  // quarters below d0 are not read
       };
       const long long nchunks = (len + 31) >> 5;
       bool in_a = false, in_b = false;
       int q_a = p, q_b = p;
       float acc_a = 0.f, acc_b = 0.f;
-      __syncwarp();  // the previous pair's reads of the query slot are done
-      if (lane < 12) {  // 4 x 16 B of coordinates, 8 x 16 B of windows
-        if (lane < 4)
-          async_copy16(reinterpret_cast<unsigned char*>(sh.qx[wb]) + 16 * lane,
-                       reinterpret_cast<const unsigned char*>(a.xrow + (size_t)p * kRowSlots) + 16 * lane);
-        else
-          async_copy16(reinterpret_cast<unsigned char*>(sh.qwin[wb]) + 16 * (lane - 4),
-                       reinterpret_cast<const unsigned char*>(a.win + (size_t)p * kRowSlots * 2) + 16 * (lane - 4));
-      }
-      async_commit();  // group: the query row
+      float4 xa[4], xb[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) xa[t] = xb[t] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (nchunks > 0) {
         fetch(lane, in_a, q_a, acc_a);
-        copy_row(slot0, in_a, q_a);
+        load_row(xa, in_a, q_a);
       }
-      async_commit();  // group: the rows of chunk 0
       if (nchunks > 1) fetch(32 + lane, in_b, q_b, acc_b);
-      async_wait<1>();  // the query row has landed
-      __syncwarp();     // ... and is visible to the whole warp
+      __syncwarp();  // the query slot is visible to the whole warp
       for (long long k = 0; k < nchunks; ++k) {
         // chunk k + 1: rows in flight; chunk k + 2: ids and distances in flight
-        if (k + 1 < nchunks) copy_row((k & 1) ? slot0 : slot1, in_b, q_b);
-        async_commit();
+        if (k + 1 < nchunks) load_row(xb, in_b, q_b);
         const bool in = in_a;
         const int q = q_a;
         const float acc = acc_a;
@@ -443,21 +428,16 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
         q_a = q_b;
         acc_a = acc_b;
         if (k + 2 < nchunks) fetch(((k + 2) << 5) + lane, in_b, q_b, acc_b);
-        async_wait<1>();  // this lane's copy of chunk k is in its slot
-        const unsigned char* slot = (k & 1) ? slot1 : slot0;
-        const float4 x0 = *reinterpret_cast<const float4*>(slot);
-        const float4 x1 = *reinterpret_cast<const float4*>(slot + 16);
-        const float4 x2 = *reinterpret_cast<const float4*>(slot + 32);
-        const float4 x3 = *reinterpret_cast<const float4*>(slot + 48);
-        const float xq[kRowSlots] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
-                                     x2.x, x2.y, x2.z, x2.w, x3.x, x3.y, x3.z, x3.w};
+        const float xq[kRowSlots] = {xa[0].x, xa[0].y, xa[0].z, xa[0].w, xa[1].x, xa[1].y, xa[1].z, xa[1].w,
+                                     xa[2].x, xa[2].y, xa[2].z, xa[2].w, xa[3].x, xa[3].y, xa[3].z, xa[3].w};
         const bool live = in && q != p;
 #pragma unroll
         for (int D = 0; D < kRowSlots; ++D) {
           const int c = D - D0;
           if (c < 0 || c >= nc) continue;  // warp-uniform
-          const float acc2 = dist_step(acc, qx[D], xq[D]);
-          const bool ok = live && xq[D] >= qwin[D][0] && xq[D] < qwin[D][1] && acc2 <= a.acc_max;
+          const float4 v = qv[D];
+          const float acc2 = dist_step(acc, v.x, xq[D]);
+          const bool ok = live && xq[D] >= v.y && xq[D] < v.z && acc2 <= a.acc_max;
           const unsigned m = __ballot_sync(0xffffffffu, ok);
           if (!m) continue;
           if (kWrite) {
@@ -472,25 +452,29 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
           }
           if ((int)lane == c) run += __popc(m);
         }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) xa[t] = xb[t];
       }
       if (!kWrite || single) {
+        int out = 0;
         if ((int)lane < nc) {
           a.cnt[item_c] = run;
           if (single) a.cap_loff[item_c] = ob;
-          n_out += (unsigned long long)run;
+          out = run;
         }
-        n_cand += (unsigned long long)len * nc;
-        n_list += (unsigned long long)len;
+        for (int o = 16; o > 0; o >>= 1) out += __shfl_xor_sync(0xffffffffu, out, o);
+        if (lane == 0) {
+          sstat[wb][0] += (unsigned long long)len * nc;
+          sstat[wb][1] += (unsigned long long)len;
+          sstat[wb][2] += (unsigned long long)out;
+        }
       }
     }
   }
-  if (!kWrite || single) {
-    for (int o = 16; o > 0; o >>= 1) n_out += __shfl_xor_sync(0xffffffffu, n_out, o);
-    if (lane == 0) {
-      if (a.cand_counter) atomicAdd(a.cand_counter, n_cand);
-      if (a.list_counter) atomicAdd(a.list_counter, n_list);
-      if (single && a.out_counter) atomicAdd(a.out_counter, n_out);
-    }
+  if ((!kWrite || single) && lane == 0) {
+    if (a.cand_counter) atomicAdd(a.cand_counter, sstat[wb][0]);
+    if (a.list_counter) atomicAdd(a.list_counter, sstat[wb][1]);
+    if (single && a.out_counter) atomicAdd(a.out_counter, sstat[wb][2]);
   }
 }
 

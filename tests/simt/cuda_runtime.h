@@ -35,6 +35,7 @@ struct alignas(16) float4 {
 struct alignas(16) uint4 {
   unsigned x, y, z, w;
 };
+inline float4 make_float4(float x, float y, float z, float w) { return float4{x, y, z, w}; }
 inline int2 make_int2(int a, int b) { return int2{a, b}; }
 using std::max;
 using std::min;
