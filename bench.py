@@ -11,9 +11,10 @@ clustered per second (n / run time) and ms per run.
              the engine's stream, L2 flushed (256 MiB write) before every step;
   e2e     -- the reference-facing call with host buffers (inscy_run: host X in,
              host labels out), host clock, copies included;
-  roofline-- the density pass-1 kernel (the dominant kernel): algorithmic bytes
-             per launch / its average launch time, against the measured HBM
-             copy bandwidth;
+  roofline-- the density candidate pass (k_neighbours_rows, the dominant
+             kernel; its level-1 counterpart is one of the averaged launches):
+             algorithmic bytes per launch / its average launch time, against
+             the measured HBM copy bandwidth;
   cpu_baseline -- the CPU restatement of the reference CPU INSCY (oracle/) on a
              bounded sample of the workload, all host cores.
 
@@ -269,7 +270,7 @@ def main():
         e2e_times.append(time.perf_counter() - t0)
     e2e_ms = 1000.0 * float(np.mean(e2e_times))
     same = s2 == subs and np.array_equal(l2, labels)
-    # ---- roofline of the density pass-1 kernel
+    # ---- roofline of the density candidate pass (pass-1 launches)
     st = stats_all[-1]
     peak, peak_kind = measured_peak()
     launches = max(1, st["density_launches_pass1"])
@@ -283,7 +284,8 @@ def main():
             traffic = json.load(open(tpath)).get("bytes_per_launch")
         except (OSError, ValueError):
             traffic = None
-    roof = {"bound": "hbm", "kernel": "k_density<pass1>", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    roof = {"bound": "hbm", "kernel": "k_neighbours_rows<write> (density candidate pass)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
             "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
     # ---- label check against the oracle at a reduced size is done by the tests;

@@ -922,14 +922,16 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       // id, list offset and length, own coordinate and fine cell, count out);
       // per list entry read 8 B (id + partial distance; at level 1 id +
       // coordinate); per further (candidate, child subspace) test at levels
-      // >= 2 5 B (the candidate's coordinate and fine cell on that dim); per
-      // entry written by the single pass 8 B
+      // >= 2 the candidate's coordinate on that dim, 4 B (the row kernel tests
+      // the fine cell as a window on the coordinate), or coordinate and fine
+      // cell, 5 B (the general kernel); per entry written by the single pass 8 B
       auto count_bytes = [&](bool single) {
         unsigned long long nc[3];
         d2h(nc, dcand_cnt, sizeof(nc), s);
         stats_.candidates += (long long)nc[0];
         stats_.density_bytes += 26.0 * (double)nitems + 8.0 * (double)nc[1] +
-                                (level == 1 ? 0.0 : 5.0 * (double)nc[0]) + (single ? 8.0 * (double)nc[2] : 0.0);
+                                (level == 1 ? 0.0 : (DL.xrow ? 4.0 : 5.0) * (double)nc[0]) +
+                                (single ? 8.0 * (double)nc[2] : 0.0);
       };
 
       // ---- 3. ordered lists of every item, then densities and flags.  At
