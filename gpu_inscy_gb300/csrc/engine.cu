@@ -637,6 +637,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   float* dxrow = nullptr;
   float* dwin = nullptr;
   unsigned long long* dwork = persist.get<unsigned long long>(1);
+  unsigned long long* dphiwork = persist.get<unsigned long long>(kPhiWorkBytes / 8);
   if (kDensityRows && d <= kRowSlots) {
     // fine_lo[k]: the least float x in [0, 1] whose fine cell before the cap,
     // (int)(x / fsz), is >= k (+inf if none); the cell is monotone in x, so
@@ -910,6 +911,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.win = dwin;
       DL.work = dxrow ? dwork : nullptr;
       DL.items = nullptr;
+      DL.phi_work = dphiwork;
       auto neighbours = [&](bool write) {
         if (level == 1) {
           launch_neighbours(DL, write, s);
@@ -975,8 +977,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
           DL.cap_loff = nullptr;
           DL.cand_counter = DL.list_counter = DL.out_counter = nullptr;
           DL.loff = dloff;
-          stats_.ms_density += timed(s, [&] { launch_density_flags(DL, s); });
-          ++launches;
+          float* dphi = lv.get<float>(nitems);
+          int* dperm = lv.get<int>(nitems);
+          CK(cudaMemsetAsync(dphiwork, 0, kPhiWorkBytes, s));
+          stats_.ms_density += timed(s, [&] { launch_density_flags(DL, dphi, dperm, s); });
+          launches += hp.rect ? 1 : 5;
         }
       }
       if (!single) {
@@ -997,11 +1002,14 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         DL.lids = lids;
         DL.lacc = lacc;
         DL.total = L;
+        float* dphi = lv.get<float>(nitems);
+        int* dperm = lv.get<int>(nitems);
+        CK(cudaMemsetAsync(dphiwork, 0, kPhiWorkBytes, s));
         stats_.ms_density += timed(s, [&] {
           neighbours(true);
-          launch_density_flags(DL, s);
+          launch_density_flags(DL, dphi, dperm, s);
         });
-        launches += 2;
+        launches += hp.rect ? 2 : 6;
       }
       // kept items
       int* dkcnt = lv.get<int>(nitems);

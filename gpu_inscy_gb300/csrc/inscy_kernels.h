@@ -66,13 +66,18 @@ struct DensityLaunch {
   const float* win;                 // d <= kRowSlots: fine-cell windows [lo, hi) per (point, dim)
   unsigned long long* work;         // work counter of the row kernel (the caller zeroes it before each launch)
   RowItem* items;                   // row kernel: one record per (group, query), written by the capacity kernel
+  unsigned long long* phi_work;     // scratch of the phi kernels (kPhiWorkBytes, zeroed by the caller before each launch)
   long long prev_total;
   long long total;
   long long prev_nkeep;
   Guard guard;
 };
 void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s);
-void launch_density_flags(const DensityLaunch& L, cudaStream_t s);
+// phi of every item (non-rectangular; `phi` holds nitems floats, `perm`
+// nitems ints), then its flags and bitmap bits.  L.phi_work points at
+// kPhiWorkBytes of zeroed scratch (the work counter and the class counts).
+constexpr int kPhiWorkBytes = 8 + 2 * 64 * 4;
+void launch_density_flags(const DensityLaunch& L, float* phi, int* perm, cudaStream_t s);
 void launch_list_capacity(const DensityLaunch& L, long long nwarps, long long* cap, cudaStream_t s);
 void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
 void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s);

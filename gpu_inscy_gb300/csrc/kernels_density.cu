@@ -526,77 +526,234 @@ __global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
   a.items[w] = r;
 }
 
-// density of every (subspace, point) from its list.  The phi sum of one item
-// is sequential, so each lane walks its own list; lists differ a lot in
-// length, so every warp owns `per_warp` consecutive items as a queue: a lane
-// that finishes an item takes the next one, and all busy lanes advance
-// together for as many entries as the shortest remaining list allows.  The
-// queue length is chosen so that the level still fills the GPU with warps
-// (32 items, one per lane, when there are few; up to 256).
-constexpr int kFlagsMaxItems = 256;
-constexpr long long kFlagsWarpsWanted = 152LL * 48;  // SMs x resident warps to aim for
+// Density of every (subspace, point) from its list, in two kernels:
+//
+// k_density_phi: the phi sum of one item is sequential, so each lane walks
+// its own list, and all busy lanes of a warp advance together for as many
+// entries as the shortest remaining list allows.  Lists differ a lot in
+// length, so (1) the items are taken in the order of a permutation that
+// groups them by list length (half-octave classes, longest first: the lanes
+// of a warp hold lists of similar length, and the longest start first), and
+// (2) lanes are refilled as they finish: the warps are persistent and take
+// batches of 32 consecutive positions of the permutation (the first one by a
+// fixed spread over the blocks, the rest from a work counter),
+// one item's (length, list start) per lane, handed to the lanes that need one
+// by shuffles; a warp stops taking batches once the counter has passed the
+// last position and finishes the items its lanes hold.
+//
+// k_density_flags: one thread per item turns the sum (or, for rectangular
+// density, the neighbour count) into the weak / dense / keep flags and sets
+// the point's bits in the subspace's bitmaps: the items of a warp are
+// consecutive, so the points that share a bitmap word are adjacent lanes,
+// and one lane per word ORs their bits in.
+constexpr int kPhiBlocksPerSM = 6;
+constexpr int kPhiClasses = 64;  // list-length classes of the permutation
 
-__device__ __forceinline__ void flags_finish(const DensityArgs& a, long long item, float v) {
-  const int si = find_sub(a.subs, a.nsubs, item);
-  const SubDesc& S = a.subs[si];
-  const long long i = item - S.item_off;
-  const int p = S.parent < 0 ? (int)i : a.prev_keep[S.query_off + i];
-  uint8_t f = 0;
-  if (v >= a.thr_weak) f |= kFlagWeak;
-  if (v >= a.thr_dense[S.nsub]) f |= kFlagDense;
-  if (v >= a.thr_keep[S.nsub]) f |= kFlagKeep;
-  a.flags[item] = f;
-  const unsigned bit = 1u << (p & 31);
-  unsigned* bm = a.bitmaps + S.bitmap_off + (p >> 5);
-  if (f & kFlagWeak) atomicOr(bm, bit);
-  if (f & kFlagDense) atomicOr(bm + a.words, bit);
-  if (f & kFlagKeep) atomicOr(bm + 2 * a.words, bit);
+// class of a list of length c: two per octave of c + 1, longest first
+__device__ __forceinline__ int phi_class(int c) {
+  const unsigned v = (unsigned)c + 1u;
+  const int lg = 31 - __clz((int)v);
+  const int half = lg >= 1 ? (int)((v >> (lg - 1)) & 1u) : 0;
+  const int k = 2 * lg + half;
+  return kPhiClasses - 1 - (k < kPhiClasses - 1 ? k : kPhiClasses - 1);
 }
 
-__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a, int per_warp) {
-  const long long first = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * per_warp;
-  if (first >= a.nitems) return;  // whole warps
-  const long long last = first + per_warp < a.nitems ? first + per_warp : a.nitems;
+// per-class item counts (hist[kPhiClasses], zeroed by the caller)
+__global__ void k_phi_class_count(const int* __restrict__ cnt, long long nitems, int* __restrict__ hist) {
+  __shared__ int local[kPhiClasses];
+  if (threadIdx.x < kPhiClasses) local[threadIdx.x] = 0;
+  __syncthreads();
+  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (it < nitems) atomicAdd(&local[phi_class(cnt[it])], 1);
+  __syncthreads();
+  if (threadIdx.x < kPhiClasses && local[threadIdx.x]) atomicAdd(&hist[threadIdx.x], local[threadIdx.x]);
+}
+
+// class starts: cursor[k] = items of the classes before k (one block)
+__global__ void k_phi_class_starts(const int* __restrict__ hist, int* __restrict__ cursor) {
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int k = 0; k < kPhiClasses; ++k) {
+      cursor[k] = o;
+      o += hist[k];
+    }
+  }
+}
+
+// scatter the items into their classes (the order within a class is free:
+// every item's sum is stored at its own index)
+__global__ void k_phi_class_scatter(const int* __restrict__ cnt, long long nitems, int* __restrict__ cursor,
+                                    int* __restrict__ perm) {
+  __shared__ int local[kPhiClasses], base[kPhiClasses];
+  if (threadIdx.x < kPhiClasses) local[threadIdx.x] = 0;
+  __syncthreads();
+  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = it < nitems ? phi_class(cnt[it]) : 0;
+  const int r = it < nitems ? atomicAdd(&local[k], 1) : 0;
+  __syncthreads();
+  if (threadIdx.x < kPhiClasses && local[threadIdx.x]) base[threadIdx.x] = atomicAdd(&cursor[threadIdx.x], local[threadIdx.x]);
+  __syncthreads();
+  if (it < nitems) perm[base[k] + r] = (int)it;
+}
+
+__global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArgs a, const int* __restrict__ perm,
+                                                                       float* __restrict__ phi) {
   const unsigned lane = lane_id();
-  long long next = first + 32;  // next item of the queue (the same in every lane)
-  long long item = first + lane;
+  const long long nitems = a.nitems;
+  // the current batch: positions bbase .. bbase + 31 of the permutation, lane
+  // l holding the item at bbase + l (bi) and its list; positions below bpos
+  // are handed out
+  long long bbase = 0;
+  int bc = 0, bpos = 32, bi = 0;
+  long long bl = 0;
+  bool drained = false;  // the counter has passed the last item (warp-uniform)
+  // the first batch of warp i of block b is batch i * gridDim.x + b, so the
+  // longest lists (the first batches) spread over the blocks and thus the
+  // SMs; later batches come from the counter, after the first gridDim.x * 8
+  bool first = true;
+  auto new_batch = [&]() {
+    long long batch;
+    if (first) {
+      batch = (long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+      first = false;
+    } else {
+      unsigned long long t = 0;
+      if (lane == 0) t = atomicAdd(a.work, 1ull);
+      batch = (long long)__shfl_sync(0xffffffffu, t, 0) + (long long)gridDim.x * (blockDim.x >> 5);
+    }
+    bbase = batch * 32;
+    drained = bbase + 32 >= nitems;
+    const long long pos = bbase + lane;
+    bi = pos < nitems ? perm[pos] : 0;
+    bc = pos < nitems ? a.cnt[bi] : 0;
+    bl = pos < nitems ? a.loff[bi] : 0;
+    bpos = 0;
+  };
+  long long item = 0;
   const float* acc = nullptr;
   int c = 0, j = 0;
   float sum = 0.f;
-  bool live = false;  // this lane holds an item whose flags are still to be written
-  auto take = [&](long long it) {
-    item = it;
-    live = false;
-    if (it >= last) return;
-    c = a.cnt[it];
-    const long long lo = a.loff[it];
-    if (!GUARD_OK(a.guard, c >= 0 && lo >= 0 && lo + c <= a.total, 41, lo + c)) return;
-    acc = a.lacc + lo;
-    j = a.rect ? c : 0;  // rectangular density: the neighbour count, no sum
-    sum = 0.f;
-    live = true;
+  bool live = false;  // this lane holds an item whose sum is still to be stored
+  // hand the next items of the queue to the lanes in `need`, in lane order
+  auto hand_out = [&](unsigned need) {
+    const int k = __popc(need & lanemask_lt());
+    const int tot = __popc(need);
+    const int avail = 32 - bpos;
+    const bool cur = k < avail;  // from the current batch, else from the next one
+    const int s0 = cur ? bpos + k : 0;
+    const int c0 = __shfl_sync(0xffffffffu, bc, s0);
+    const long long l0 = __shfl_sync(0xffffffffu, bl, s0);
+    const int x0 = __shfl_sync(0xffffffffu, bi, s0);
+    const bool v0 = bbase + s0 < nitems;
+    int c1 = 0, x1 = 0;
+    long long l1 = 0;
+    bool v1 = false;
+    if (tot > avail) {
+      if (!drained) {
+        new_batch();
+        const int s1 = cur ? 0 : k - avail;
+        c1 = __shfl_sync(0xffffffffu, bc, s1);
+        l1 = __shfl_sync(0xffffffffu, bl, s1);
+        x1 = __shfl_sync(0xffffffffu, bi, s1);
+        v1 = bbase + s1 < nitems;
+        bpos = tot - avail;
+      } else {
+        bpos = 32;
+      }
+    } else {
+      bpos += tot;
+    }
+    if ((need >> lane) & 1u) {
+      item = cur ? x0 : x1;
+      c = cur ? c0 : c1;
+      const long long lo = cur ? l0 : l1;
+      live = (cur ? v0 : v1) && GUARD_OK(a.guard, c >= 0 && lo >= 0 && lo + c <= a.total, 41, lo + c);
+      acc = a.lacc + lo;
+      j = 0;
+      sum = 0.f;
+    }
   };
-  take(item);
+  new_batch();
+  hand_out(0xffffffffu);
   for (;;) {
     if (!__any_sync(0xffffffffu, live)) break;
     // steps every busy lane can take: the shortest remaining list
     int steps = live ? c - j : INT_MAX;
     for (int o = 16; o > 0; o >>= 1) steps = min(steps, __shfl_xor_sync(0xffffffffu, steps, o));
     if (live) {
-      for (int t = 0; t < steps; ++t) {
-        const float dd = __fdiv_rn(__fsqrt_rn(acc[j + t]), a.eps);
-        sum = phi_step_exact(sum, __fmul_rn(dd, dd));  // integer pipe, no FP64
+      // the terms do not depend on the sum: four at a time are loaded and
+      // computed side by side, then added in order (the sum's chain alone is
+      // sequential)
+      const float* ap = acc + j;
+      int t = 0;
+      for (; t + 4 <= steps; t += 4) {
+        const float a0 = ap[t], a1 = ap[t + 1], a2 = ap[t + 2], a3 = ap[t + 3];
+        const float d0 = __fdiv_rn(__fsqrt_rn(a0), a.eps), d1 = __fdiv_rn(__fsqrt_rn(a1), a.eps);
+        const float d2 = __fdiv_rn(__fsqrt_rn(a2), a.eps), d3 = __fdiv_rn(__fsqrt_rn(a3), a.eps);
+        sum = phi_step_exact(sum, __fmul_rn(d0, d0));  // integer pipe, no FP64
+        sum = phi_step_exact(sum, __fmul_rn(d1, d1));
+        sum = phi_step_exact(sum, __fmul_rn(d2, d2));
+        sum = phi_step_exact(sum, __fmul_rn(d3, d3));
+      }
+      for (; t < steps; ++t) {
+        const float dd = __fdiv_rn(__fsqrt_rn(ap[t]), a.eps);
+        sum = phi_step_exact(sum, __fmul_rn(dd, dd));
       }
       j += steps;
     }
     const bool done = live && j >= c;
-    if (done) flags_finish(a, item, a.rect ? (float)c : sum);
-    const unsigned need = __ballot_sync(0xffffffffu, done || (!live && item < last));
-    if (need) {
-      const long long mine = next + __popc(need & lanemask_lt());
-      if ((need >> lane) & 1u) take(mine);
-      next += __popc(need);
+    if (done) {
+      phi[item] = sum;
+      live = false;
     }
+    // lanes without an item ask for one while the queue lasts
+    const bool more = !(drained && bpos >= 32) ;
+    const unsigned need = __ballot_sync(0xffffffffu, more && !live);
+    if (need) hand_out(need);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_density_flags(DensityArgs a, const float* __restrict__ phi) {
+  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if ((it & ~31LL) >= a.nitems) return;  // whole warps
+  const unsigned lane = lane_id();
+  const bool valid = it < a.nitems;
+  const long long itc = valid ? it : a.nitems - 1;
+  const int si = find_sub(a.subs, a.nsubs, itc);
+  const SubDesc& S = a.subs[si];
+  const long long i = itc - S.item_off;
+  const int p = S.parent < 0 ? (int)i : a.prev_keep[S.query_off + i];
+  uint8_t f = 0;
+  if (valid && GUARD_OK(a.guard, p >= 0 && p < a.n, 42, p)) {
+    const float v = a.rect ? (float)a.cnt[it] : phi[it];
+    if (v >= a.thr_weak) f |= kFlagWeak;
+    if (v >= a.thr_dense[S.nsub]) f |= kFlagDense;
+    if (v >= a.thr_keep[S.nsub]) f |= kFlagKeep;
+    a.flags[it] = f;
+  }
+  // the word of the point in its subspace's bitmaps; adjacent lanes share it
+  // (items of a subspace ascend in point), so OR the bits over each run of
+  // equal words and let the run's last lane store them
+  const long long word = valid ? S.bitmap_off + (p >> 5) : -1 - (long long)lane;
+  const unsigned bit = 1u << (p & 31);
+  unsigned w = (f & kFlagWeak) ? bit : 0u, dn = (f & kFlagDense) ? bit : 0u, kp = (f & kFlagKeep) ? bit : 0u;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long wo = __shfl_up_sync(0xffffffffu, word, o);
+    const unsigned a0 = __shfl_up_sync(0xffffffffu, w, o);
+    const unsigned a1 = __shfl_up_sync(0xffffffffu, dn, o);
+    const unsigned a2 = __shfl_up_sync(0xffffffffu, kp, o);
+    if ((int)lane >= o && wo == word) {
+      w |= a0;
+      dn |= a1;
+      kp |= a2;
+    }
+  }
+  const long long wn = __shfl_sync(0xffffffffu, word, lane < 31 ? (int)lane + 1 : 31);
+  if (valid && (lane == 31 || wn != word)) {
+    unsigned* bm = a.bitmaps + word;
+    if (w) atomicOr(bm, w);
+    if (dn) atomicOr(bm + a.words, dn);
+    if (kp) atomicOr(bm + 2 * a.words, kp);
   }
 }
 
@@ -807,13 +964,22 @@ void launch_list_capacity(const DensityLaunch& L, long long nwarps, long long* c
   k_list_capacity<<<(unsigned)((nwarps + 255) / 256), 256, 0, s>>>(a, cap);
 }
 
-void launch_density_flags(const DensityLaunch& L, cudaStream_t s) {
+void launch_density_flags(const DensityLaunch& L, float* phi, int* perm, cudaStream_t s) {
   if (L.nitems <= 0) return;
   DensityArgs a = make_args(L);
-  long long per_warp = (L.nitems / kFlagsWarpsWanted + 31) / 32 * 32;
-  per_warp = per_warp < 32 ? 32 : per_warp > kFlagsMaxItems ? kFlagsMaxItems : per_warp;
-  const long long warps = (L.nitems + per_warp - 1) / per_warp;
-  k_density_flags<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(a, (int)per_warp);
+  if (!L.rect) {  // rectangular density compares the neighbour count: no sum
+    a.work = L.phi_work;
+    int* hist = reinterpret_cast<int*>(L.phi_work + 1);  // kPhiClasses counts, then kPhiClasses cursors
+    const unsigned iblocks = (unsigned)((L.nitems + 255) / 256);
+    k_phi_class_count<<<iblocks, 256, 0, s>>>(L.cnt, L.nitems, hist);
+    k_phi_class_starts<<<1, 32, 0, s>>>(hist, hist + kPhiClasses);
+    k_phi_class_scatter<<<iblocks, 256, 0, s>>>(L.cnt, L.nitems, hist + kPhiClasses, perm);
+    const long long need = (L.nitems + 255) / 256;  // one 32-item batch per warp
+    const long long cap = 152LL * kPhiBlocksPerSM;
+    const unsigned blocks = (unsigned)(need < cap ? need : cap);
+    k_density_phi<<<blocks, 256, 0, s>>>(a, perm, phi);
+  }
+  k_density_flags<<<(unsigned)((L.nitems + 255) / 256), 256, 0, s>>>(a, phi);
 }
 
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
