@@ -71,8 +71,8 @@ const double kPi = 3.14;  // ClusteringCpu.cu:27
 #define INSCY_SINGLE_PASS_BYTES (32LL << 30)
 #endif
 constexpr long long kSinglePassBytes = INSCY_SINGLE_PASS_BYTES;
-// density pass over point rows (k_neighbours_rows) when d <= kRowSlots; 0
-// keeps the general kernel for every d (both give the same lists)
+// density pass over point rows (k_neighbours_rows) when d <= 32; 0 keeps the
+// general kernel for every d (both give the same lists)
 #ifndef INSCY_DENSITY_ROWS
 #define INSCY_DENSITY_ROWS 1
 #endif
@@ -633,12 +633,13 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   };
   launch_prep(dX, ni, d, cells, csz, G, fsz, hp.eps, dcc, dfc, dgz, s);
   ++launches;
-  // point rows for the density pass when a row fits kRowSlots slots
+  // point rows for the density pass when a row fits 16 or 32 slots
   float* dxrow = nullptr;
   float* dwin = nullptr;
   unsigned long long* dwork = persist.get<unsigned long long>(1);
   unsigned long long* dphiwork = persist.get<unsigned long long>(kPhiWorkBytes / 8);
-  if (kDensityRows && d <= kRowSlots) {
+  const int slots = kDensityRows ? row_slots(d) : 0;
+  if (slots) {
     // fine_lo[k]: the least float x in [0, 1] whose fine cell before the cap,
     // (int)(x / fsz), is >= k (+inf if none); the cell is monotone in x, so
     // the +-1 fine-cell test becomes an interval test on the coordinate
@@ -666,9 +667,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     }
     float* dfine = persist.get<float>(G + 2);
     h2d(dfine, fine_lo.data(), sizeof(float) * (G + 2), s);
-    dxrow = persist.get<float>((size_t)n * kRowSlots);
-    dwin = persist.get<float>((size_t)n * kRowSlots * 2);
-    launch_point_rows(dX, dfc, ni, d, G, dfine, dxrow, dwin, s);
+    dxrow = persist.get<float>((size_t)n * slots);
+    dwin = persist.get<float>((size_t)n * slots * 2);
+    launch_point_rows(dX, dfc, ni, d, slots, G, dfine, dxrow, dwin, s);
     ++launches;
   }
   int* drank = persist.get<int>(n);
@@ -909,6 +910,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.cap_loff = nullptr;
       DL.xrow = dxrow;
       DL.win = dwin;
+      DL.slots = slots;
       DL.work = dxrow ? dwork : nullptr;
       DL.items = nullptr;
       DL.phi_work = dphiwork;

@@ -69,11 +69,12 @@ struct DensityArgs {
   // its length; the kernel writes every item's count and list start (cap_loff)
   const long long* cap_base;
   long long* cap_loff;
-  // point rows (d <= kRowSlots) and the work counter of k_neighbours_rows
+  // point rows (d <= 32) and the work counter of k_neighbours_rows
   const float* xrow;
   const float* win;
   unsigned long long* work;
   RowItem* items;        // per (group, query): written by k_list_capacity, read by k_neighbours_rows
+  int slots;             // row width of xrow / win (16 or 32; 0: no rows)
   int chunk;             // (group, query) pairs a warp takes per counter update
   long long prev_total;  // entries in the previous level's lists
   long long total;       // entries in this level's lists (write passes)
@@ -325,32 +326,36 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
   }
 }
 
-// Levels >= 2 when d <= kRowSlots: the same tests and outputs as
-// k_neighbours_multi, with
+// Levels >= 2 when d <= 32 (rows of kS = 16 or 32 slots): the same tests and
+// outputs as k_neighbours_multi, with
 //   * the (group, query) pair read from its record (RowItem, resolved by
 //     k_list_capacity), so a pair starts after one load instead of a search
 //     and a chain of dependent loads;
-//   * every candidate's row of coordinates (16 floats, 64 bytes; the 16-byte
-//     quarters below the first child's dim are skipped) loaded once into
-//     registers, and the children walked by a loop over the 16 dims unrolled
-//     at compile time (a group's children extend the parent by the
+//   * every candidate's row of coordinates (kS floats; the 16-byte quarters
+//     below the first child's dim are skipped) loaded once into registers,
+//     and the children walked by a loop over the kS dims unrolled at compile
+//     time (a group's children extend the parent by the
 //     consecutive dims d0 .. d0 + nc - 1, child c = dim d0 + c), so a
 //     (candidate, child) test reads registers and one warp-uniform 16-byte
 //     shared load (the query's coordinate and fine-cell window on that dim).
 //     The +-1 fine-cell test is the equivalent interval test
 //     lo_p <= x_q < hi_p, so no fine cell of the candidate is read;
 //   * a software pipeline over the 32-candidate chunks of a list: the ids and
-//     partial distances of chunk k + 2 and the rows of chunk k + 1 are loaded
-//     while chunk k is tested;
+//     partial distances of chunk k + 2 and (kS = 16; 32-slot rows take too
+//     many registers to hold two) the rows of chunk k + 1 are loaded while
+//     chunk k is tested;
 //   * warps taking `chunk` (group, query) pairs at a time from a work counter,
 //     so a warp whose list was short takes the next pair instead of idling
 //     until the longest list of its block is done.
-constexpr int kRowsBlocksPerSM = 4;
 constexpr int kRowsSMs = 152;
+// resident blocks per SM: 64 registers a thread for 16-slot rows, 80 for 32
+constexpr int rows_blocks_per_sm(int slots) { return slots == 16 ? 4 : 3; }
 
-template <bool kWrite>
-__global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(DensityArgs a) {
-  __shared__ float4 squery[8][kRowSlots];  // per warp and dim: the query's (x, lo, hi, -)
+template <bool kWrite, int kS>
+__global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows(DensityArgs a) {
+  constexpr int kQ = kS / 4;           // 16-byte quarters of a row
+  constexpr bool kPre = kS == 16;      // rows of the next chunk held in registers
+  __shared__ float4 squery[8][kS];     // per warp and dim: the query's (x, lo, hi, -)
   // per warp: candidate tests, list entries read, entries written; added to
   // the global counters once when the warp exits (per-pair atomics on three
   // adjacent counters saturate one L2 slice)
@@ -384,8 +389,8 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
         if ((int)lane < nc) ob = a.loff[item_c];
       }
       __syncwarp();  // the previous pair's reads of the query slot are done
-      if (lane < (unsigned)kRowSlots) {
-        const size_t t = (size_t)p * kRowSlots + lane;
+      if (lane < (unsigned)kS) {
+        const size_t t = (size_t)p * kS + lane;
         squery[wb][lane] = make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
       }
       // candidate j of the list (lanes past the end stand on the query
@@ -396,31 +401,35 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
         acc = in ? accs[j] : 0.f;
       };
       // the id is checked where it is first used: the load of its row
-      auto load_row = [&](float4 (&x)[4], bool& in, int& q) {
+      auto load_row = [&](float4 (&x)[kQ], bool& in, int& q) {
         if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
           in = false;
           q = p;
         }
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-          if (4 * t + 3 >= D0) x[t] = xrow4[(size_t)q * 4 + t];  // quarters below d0 are not read
+        for (int t = 0; t < kQ; ++t)
+          if (4 * t + 3 >= D0) x[t] = xrow4[(size_t)q * kQ + t];  // quarters below d0 are not read
       };
       const long long nchunks = (len + 31) >> 5;
       bool in_a = false, in_b = false;
       int q_a = p, q_b = p;
       float acc_a = 0.f, acc_b = 0.f;
-      float4 xa[4], xb[4];
+      float4 xa[kQ], xb[kQ];  // xb: the next chunk's rows (kPre only)
 #pragma unroll
-      for (int t = 0; t < 4; ++t) xa[t] = xb[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int t = 0; t < kQ; ++t) xa[t] = xb[t] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (nchunks > 0) {
         fetch(lane, in_a, q_a, acc_a);
-        load_row(xa, in_a, q_a);
+        if (kPre) load_row(xa, in_a, q_a);
       }
       if (nchunks > 1) fetch(32 + lane, in_b, q_b, acc_b);
       __syncwarp();  // the query slot is visible to the whole warp
       for (long long k = 0; k < nchunks; ++k) {
-        // chunk k + 1: rows in flight; chunk k + 2: ids and distances in flight
-        if (k + 1 < nchunks) load_row(xb, in_b, q_b);
+        // chunk k + 1: rows in flight (kPre); chunk k + 2: ids and distances in flight
+        if (kPre) {
+          if (k + 1 < nchunks) load_row(xb, in_b, q_b);
+        } else {
+          load_row(xa, in_a, q_a);
+        }
         const bool in = in_a;
         const int q = q_a;
         const float acc = acc_a;
@@ -428,16 +437,23 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
         q_a = q_b;
         acc_a = acc_b;
         if (k + 2 < nchunks) fetch(((k + 2) << 5) + lane, in_b, q_b, acc_b);
-        const float xq[kRowSlots] = {xa[0].x, xa[0].y, xa[0].z, xa[0].w, xa[1].x, xa[1].y, xa[1].z, xa[1].w,
-                                     xa[2].x, xa[2].y, xa[2].z, xa[2].w, xa[3].x, xa[3].y, xa[3].z, xa[3].w};
+        float xq[kS];
+#pragma unroll
+        for (int t = 0; t < kQ; ++t) {
+          xq[4 * t] = xa[t].x;
+          xq[4 * t + 1] = xa[t].y;
+          xq[4 * t + 2] = xa[t].z;
+          xq[4 * t + 3] = xa[t].w;
+        }
         const bool live = in && q != p;
 #pragma unroll
-        for (int D = 0; D < kRowSlots; ++D) {
+        for (int D = 0; D < kS; ++D) {
           const int c = D - D0;
           if (c < 0 || c >= nc) continue;  // warp-uniform
           const float4 v = qv[D];
-          const float acc2 = dist_step(acc, v.x, xq[D]);
-          const bool ok = live && xq[D] >= v.y && xq[D] < v.z && acc2 <= a.acc_max;
+          const float xd = xq[D];
+          const float acc2 = dist_step(acc, v.x, xd);
+          const bool ok = live && xd >= v.y && xd < v.z && acc2 <= a.acc_max;
           const unsigned m = __ballot_sync(0xffffffffu, ok);
           if (!m) continue;
           if (kWrite) {
@@ -452,8 +468,10 @@ __global__ void __launch_bounds__(256, kRowsBlocksPerSM) k_neighbours_rows(Densi
           }
           if ((int)lane == c) run += __popc(m);
         }
+        if (kPre) {
 #pragma unroll
-        for (int t = 0; t < 4; ++t) xa[t] = xb[t];
+          for (int t = 0; t < kQ; ++t) xa[t] = xb[t];
+        }
       }
       if (!kWrite || single) {
         int out = 0;
@@ -514,7 +532,7 @@ __global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
     const long long pb = a.prev_loff[k];
     const int nc = g.nchild, d0 = a.subs[g.sub_base].dim;
     if (GUARD_OK(a.guard,
-                 d0 >= 0 && nc >= 1 && d0 + nc <= kRowSlots && a.subs[g.sub_base + nc - 1].dim == d0 + nc - 1, 37,
+                 d0 >= 0 && nc >= 1 && d0 + nc <= a.slots && a.subs[g.sub_base + nc - 1].dim == d0 + nc - 1, 37,
                  d0) &&
         GUARD_OK(a.guard, p >= 0 && p < a.n, 32, p) &&
         GUARD_OK(a.guard, pb >= 0 && len >= 0 && pb + len <= a.prev_total, 33, pb + len)) {
@@ -879,6 +897,7 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.win = L.win;
   a.work = L.work;
   a.items = L.items;
+  a.slots = L.slots;
   a.chunk = 1;
   a.prev_total = L.prev_total;
   a.total = L.total;
@@ -936,18 +955,25 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
   if (nwarps <= 0) return;
   DensityArgs a = make_args(L);
   a.nwarps = nwarps;
-  if (L.xrow && L.win && L.work && L.items && L.d <= kRowSlots) {
+  if (L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 32) && L.d <= L.slots) {
     // persistent warps: a grid that fills every SM once, (group, query) pairs
     // handed out by the work counter, several per update when there are many
-    const long long resident = (long long)kRowsSMs * kRowsBlocksPerSM * 8;
-    long long chunk = nwarps / (resident * 16);
+    const long long max_blocks = (long long)kRowsSMs * rows_blocks_per_sm(L.slots);
+    long long chunk = nwarps / (max_blocks * 8 * 16);
     a.chunk = (int)(chunk < 1 ? 1 : chunk > 8 ? 8 : chunk);
     const long long need = (nwarps + 7) / 8;
-    const unsigned blocks = (unsigned)(need < kRowsSMs * kRowsBlocksPerSM ? need : kRowsSMs * kRowsBlocksPerSM);
-    if (write)
-      k_neighbours_rows<true><<<blocks, 256, 0, s>>>(a);
-    else
-      k_neighbours_rows<false><<<blocks, 256, 0, s>>>(a);
+    const unsigned blocks = (unsigned)(need < max_blocks ? need : max_blocks);
+    if (L.slots == 16) {
+      if (write)
+        k_neighbours_rows<true, 16><<<blocks, 256, 0, s>>>(a);
+      else
+        k_neighbours_rows<false, 16><<<blocks, 256, 0, s>>>(a);
+    } else {
+      if (write)
+        k_neighbours_rows<true, 32><<<blocks, 256, 0, s>>>(a);
+      else
+        k_neighbours_rows<false, 32><<<blocks, 256, 0, s>>>(a);
+    }
     return;
   }
   unsigned blocks = (unsigned)((nwarps * 32 + 255) / 256);

@@ -128,16 +128,17 @@ void launch_prep(const float* X, int n, int d, int cells, float csz, int G, floa
   k_prep<<<(n + 255) / 256, 256, 0, s>>>(X, n, d, cells, csz, G, fsz, eps, cc, fc, gz);
 }
 
-// Point rows of 16 slots for d <= 16: the coordinates (64 B) of every point,
+// Point rows of `slots` (16 or 32) >= d: the coordinates of every point,
 // zero-padded, and its fine-cell window per dim as a coordinate interval
 // [lo, hi) (fine_lo[k] = least x whose fine cell before the cap is >= k):
 // q is within +-1 fine cell of p on dim k iff lo_p <= x_q < hi_p.
-__global__ void k_point_rows(const float* __restrict__ X, const uint8_t* __restrict__ fc, int n, int d, int G,
-                             const float* __restrict__ fine_lo, float* __restrict__ xrow, float* __restrict__ win) {
+__global__ void k_point_rows(const float* __restrict__ X, const uint8_t* __restrict__ fc, int n, int d, int slots,
+                             int G, const float* __restrict__ fine_lo, float* __restrict__ xrow,
+                             float* __restrict__ win) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n * kRowSlots) return;
-  const long long p = t / kRowSlots;
-  const int k = (int)(t % kRowSlots);
+  if (t >= (long long)n * slots) return;
+  const long long p = t / slots;
+  const int k = (int)(t % slots);
   const float ninf = __uint_as_float(0xff800000u), pinf = __uint_as_float(0x7f800000u);
   float x = 0.f, lo = ninf, hi = pinf;
   if (k < d) {
@@ -151,10 +152,10 @@ __global__ void k_point_rows(const float* __restrict__ X, const uint8_t* __restr
   win[2 * t + 1] = hi;
 }
 
-void launch_point_rows(const float* X, const uint8_t* fc, int n, int d, int G, const float* fine_lo, float* xrow,
-                       float* win, cudaStream_t s) {
-  long long m = (long long)n * kRowSlots;
-  if (m > 0) k_point_rows<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(X, fc, n, d, G, fine_lo, xrow, win);
+void launch_point_rows(const float* X, const uint8_t* fc, int n, int d, int slots, int G, const float* fine_lo,
+                       float* xrow, float* win, cudaStream_t s) {
+  long long m = (long long)n * slots;
+  if (m > 0) k_point_rows<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(X, fc, n, d, slots, G, fine_lo, xrow, win);
 }
 
 void launch_iota(int* a, int n, cudaStream_t s) {

@@ -22,8 +22,8 @@ def small_case(rect):
     return z["X"], p, unpack(z["dims"], z["labels"])
 
 
-def family_cases():
-    z = np.load(os.path.join(GOLDEN, "family.npz"))
+def family_cases(name="family.npz"):
+    z = np.load(os.path.join(GOLDEN, name))
     out = []
     for i in range(int(z["count"])):
         v = z["params%d" % i]
@@ -32,6 +32,11 @@ def family_cases():
                  entropy_order=int(v[7]))
         out.append((i, z["X%d" % i], p, unpack(z["dims%d" % i], z["labels%d" % i])))
     return out
+
+
+def wide_cases():
+    """16 < d <= 32 (32-slot point rows), made by tests/golden/make_wide.py."""
+    return family_cases("wide.npz")
 
 
 def assert_same(got, want, what=""):

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as orc
-from golden_io import assert_same, family_cases, small_case
+from golden_io import assert_same, family_cases, small_case, wide_cases
 from gpu_inscy_gb300 import _lib, synth
 
 pytestmark = pytest.mark.gpu
@@ -35,6 +35,14 @@ def test_family_matches_reference_outputs(engine, case):
     i, X, p, want = case
     got, _ = gpu_run(X, **p)
     assert_same(got, want, "family %d" % i)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_wide_rows_match_oracle_fixtures(engine, case):
+    # 16 < d <= 32: the density pass runs on 32-slot point rows
+    i, X, p, want = wide_cases()[case]
+    got, _ = gpu_run(X, **p)
+    assert_same(got, want, "wide %d (d=%d)" % (i, X.shape[1]))
 
 
 def _random_case(seed):

@@ -15,7 +15,7 @@ import sys
 import numpy as np
 import pytest
 
-from golden_io import assert_same, family_cases, small_case
+from golden_io import assert_same, family_cases, small_case, wide_cases
 from gpu_inscy_gb300 import synth
 import oracle as orc
 
@@ -67,6 +67,12 @@ def test_family_cases(driver):
     cases = [c for c in family_cases() if c[2]["entropy_order"] == 0][:12]
     for i, X, p, want in cases:
         assert_same(simt_run(driver, X, p, i % 2 == 1, "family%d" % i), want, "family %d" % i)
+
+
+def test_wide_rows(driver):
+    # d = 20: the density pass on 32-slot point rows
+    i, X, p, want = wide_cases()[0]
+    assert_same(simt_run(driver, X, p, True, "wide0"), want, "wide %d (d=%d)" % (i, X.shape[1]))
 
 
 @pytest.fixture(scope="module")
