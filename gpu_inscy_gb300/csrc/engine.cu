@@ -1050,7 +1050,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       std::vector<long long> work_off(ncalls), work_scr;
       std::vector<int> items_big, items_small;  // work items by block size (see launch_tree_level)
       long long nwork = 0, scr = 0, pts_cap = 0, ghost_in = 0;
+      int key_bits = 0;  // widest leaf key of the level: (remaining dims incl. D) x bits per cell
       for (int i = 0; i < ncalls; ++i) {
+        key_bits = std::max(key_bits, (d - F.hcalls[i].nrestricted) * kbits);
         work_off[i] = nwork;
         int nd = d - F.hcalls[i].f;
         for (int t = 0; t < nd; ++t) {
@@ -1126,7 +1128,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         TL.pts_in_total = F.pts_total;
         TL.ghosts_in_total = F.ghosts_total;
         TL.guard = guard;
-        TL.key_bytes = std::max(kTreeMinKeyBytes, d * kbits <= 32 ? 4 : d * kbits <= 64 ? 8 : 16);
+        // a work item's leaf key holds its call's remaining dims and D: the
+        // level's widest key decides the key type
+        TL.key_bytes = std::max(kTreeMinKeyBytes, key_bits <= 32 ? 4 : key_bits <= 64 ? 8 : 16);
         TL.items_big = ditems;
         TL.nbig = ditems ? (int)items_big.size() : 0;
         TL.items_small = ditems ? ditems + items_big.size() : nullptr;
