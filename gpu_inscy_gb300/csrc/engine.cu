@@ -938,11 +938,12 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
                                 (single ? 8.0 * (double)nc[2] : 0.0);
       };
 
-      // ---- 3. ordered lists of every item, then densities and flags.  At
-      // levels >= 2 a child's list is a subsequence of the parent's, so when
-      // the parent lengths bound the level within kSinglePassBytes one pass
-      // tests and writes (lists at capacity offsets); otherwise a count pass
-      // sizes the lists exactly and a second pass writes them.
+      // ---- 3. ordered lists of every item, then densities and flags.  A
+      // list is a subsequence of a known list (the parent's at levels >= 2,
+      // the fine cell's candidates at level 1), so when those lengths bound
+      // the level within the single-pass budget one pass tests and writes
+      // (lists at capacity offsets); otherwise a count pass sizes the lists
+      // exactly and a second pass writes them.
       long long* dloff = lv.get<long long>(nitems);
       long long* dtot = lv.get<long long>(2);
       void* sums = scan_sums(std::max(std::max(nitems, (long long)nsubs * W), ngroup_warps) + 1, s, lv);
@@ -950,12 +951,19 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       int* lids = nullptr;
       float* lacc = nullptr;
       bool single = false;
-      if (level > 1) {
-        long long* cap = lv.get<long long>(ngroup_warps + 1);
-        long long* cbase = lv.get<long long>(ngroup_warps + 1);
-        if (DL.work) DL.items = lv.get<RowItem>(ngroup_warps);  // the row kernel's pair records
-        launch_list_capacity(DL, ngroup_warps, cap, s);
-        launch_exclusive_scan_ll(cap, cbase, ngroup_warps, dtot, sums, s);
+      {
+        // capacities: per (group, query) at levels >= 2, per item (the
+        // candidate-list length) at level 1
+        const long long ncap = level > 1 ? ngroup_warps : nitems;
+        long long* cap = lv.get<long long>(ncap + 1);
+        long long* cbase = lv.get<long long>(ncap + 1);
+        if (level > 1) {
+          if (DL.work) DL.items = lv.get<RowItem>(ngroup_warps);  // the row kernel's pair records
+          launch_list_capacity(DL, ngroup_warps, cap, s);
+        } else {
+          launch_level1_capacity(DL, cap, s);
+        }
+        launch_exclusive_scan_ll(cap, cbase, ncap, dtot, sums, s);
         launches += 4;
         const long long capt = scalar(dtot, s);
         if (capt * 8 <= t_single_pass_bytes) {
@@ -1263,7 +1271,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
           launch_uf_flatten(CA, is_root, root_of, s);
           launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
         });
-        launches += 8;
+        launches += 9;
         ncomp = scalar(dnc, s);
         int* dcbase = lv.get<int>(nsubs + 1);
         launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);

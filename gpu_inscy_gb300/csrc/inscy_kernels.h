@@ -80,6 +80,7 @@ void launch_neighbours(const DensityLaunch& L, bool write, cudaStream_t s);
 constexpr int kPhiWorkBytes = 8 + 2 * 64 * 4;
 void launch_density_flags(const DensityLaunch& L, float* phi, int* perm, cudaStream_t s);
 void launch_list_capacity(const DensityLaunch& L, long long nwarps, long long* cap, cudaStream_t s);
+void launch_level1_capacity(const DensityLaunch& L, long long* cap, cudaStream_t s);
 void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
 void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s);
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,

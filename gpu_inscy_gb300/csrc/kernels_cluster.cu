@@ -118,6 +118,19 @@ __global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
   }
 }
 
+// (1b) compress: every dense kept point points at its root, so the finds of
+// the sampling and of the skip test in (3) take one step
+__global__ void __launch_bounds__(256) k_uf_compress(ClusterArgs a) {
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  if (!a.clustered[si]) return;
+  const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+  if (!bit_of(dn, a.keep_ids[kk])) return;
+  const int r = uf_find(a.uf, (int)kk);
+  if (r != (int)kk) ((volatile int*)a.uf)[kk] = r;  // an ancestor: finds stay valid
+}
+
 // (2) one warp per clustered subspace: a dense point of the dominant component
 __global__ void k_uf_sample(ClusterArgs a, int nclustered, int* __restrict__ sample) {
   const int cs = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -384,6 +397,7 @@ void launch_uf_init(int* par, long long n, cudaStream_t s) {
 void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, cudaStream_t s) {
   if (a.nkeep <= 0) return;
   k_uf_link2<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a);
+  k_uf_compress<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a);
   if (nclustered > 0) k_uf_sample<<<(unsigned)((nclustered * 32LL + 255) / 256), 256, 0, s>>>(a, nclustered, sample);
   k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a, cslot_of, sample);
 }

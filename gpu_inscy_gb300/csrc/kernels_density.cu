@@ -117,30 +117,36 @@ __device__ __forceinline__ void locate(const DensityArgs& a, long long w, int& s
 // global add per block (per-warp global atomics on the same few counters
 // saturate the L2 slice that holds them).
 struct BlockStats {
-  unsigned long long cand, list;
+  unsigned long long cand, list, out;
 };
 __device__ __forceinline__ void block_stats_begin(BlockStats& s) {
-  if (threadIdx.x == 0) s.cand = s.list = 0;
+  if (threadIdx.x == 0) s.cand = s.list = s.out = 0;
   __syncthreads();
 }
 __device__ __forceinline__ void block_stats_end(BlockStats& s, const DensityArgs& a, unsigned long long cand,
-                                                unsigned long long list) {
-  if (lane_id() == 0 && (cand || list)) {
+                                                unsigned long long list, unsigned long long out = 0) {
+  if (lane_id() == 0 && (cand || list || out)) {
     atomicAdd(&s.cand, cand);
     atomicAdd(&s.list, list);
+    atomicAdd(&s.out, out);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     if (a.cand_counter && s.cand) atomicAdd(a.cand_counter, s.cand);
     if (a.list_counter && s.list) atomicAdd(a.list_counter, s.list);
+    if (a.out_counter && s.out) atomicAdd(a.out_counter, s.out);
   }
 }
 
 template <bool kWrite>
 __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
+  // single-pass write (cap_base set): the list of an item starts at
+  // cap_base[item], its candidate-list length being a bound; the kernel also
+  // writes the count and the list start (cap_loff)
+  const bool single = kWrite && a.cap_base != nullptr;
   __shared__ BlockStats bs;
-  if (!kWrite) block_stats_begin(bs);
-  unsigned long long n_len = 0;  // the warp's list length (count pass)
+  if (!kWrite || single) block_stats_begin(bs);
+  unsigned long long n_len = 0, n_out = 0;  // the warp's list length and entries written
   [&] {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= a.nwarps) return;
@@ -172,7 +178,7 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     if (!GUARD_OK(a.guard, b >= 0 && len >= 0 && b + len <= a.prev_total, 23, b + len)) return;
   }
   int count = 0;
-  const long long wbase = kWrite ? a.loff[item] : 0;
+  const long long wbase = single ? a.cap_base[item] : kWrite ? a.loff[item] : 0;
   for (long long j0 = 0; j0 < len; j0 += 32) {
     long long j = j0 + lane;
     bool ok = j < len;
@@ -199,10 +205,14 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     }
     count += __popc(m);
   }
-  if (!kWrite && lane == 0) a.cnt[item] = count;
+  if ((!kWrite || single) && lane == 0) {
+    a.cnt[item] = count;
+    if (single) a.cap_loff[item] = wbase;
+  }
   n_len = (unsigned long long)len;
+  n_out = (unsigned long long)count;
   }();
-  if (!kWrite) block_stats_end(bs, a, n_len, n_len);
+  if (!kWrite || single) block_stats_end(bs, a, n_len, n_len, single ? n_out : 0);
 }
 
 // Levels >= 2: every child subspace of a parent filters the same parent list
@@ -542,6 +552,29 @@ __global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
     }
   }
   a.items[w] = r;
+}
+
+// level 1: the capacity of item (subspace {D}, point p) is the length of the
+// candidate list of p's fine cell on D
+__global__ void k_level1_capacity(DensityArgs a, long long* __restrict__ cap) {
+  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= a.nitems) return;
+  const SubDesc& S = a.subs[find_sub(a.subs, a.nsubs, it)];
+  const long long i = it - S.item_off;
+  long long len = 0;
+  if (GUARD_OK(a.guard, S.parent < 0 && i >= 0 && i < a.n, 38, i)) {
+    const size_t c = (size_t)S.dim * a.G + a.fc[(size_t)i * a.d + S.dim];
+    len = a.cand_off[c + 1] - a.cand_off[c];
+  }
+  cap[it] = len;
+}
+
+static DensityArgs make_args(const DensityLaunch& L);
+
+void launch_level1_capacity(const DensityLaunch& L, long long* cap, cudaStream_t s) {
+  if (L.nitems <= 0) return;
+  DensityArgs a = make_args(L);
+  k_level1_capacity<<<(unsigned)((L.nitems + 255) / 256), 256, 0, s>>>(a, cap);
 }
 
 // Density of every (subspace, point) from its list, in two kernels:
