@@ -21,6 +21,11 @@ clustered per second (n / run time) and ms per run.
 batched -- the 64-dataset batch workload: plain runs one after another vs the
              batched form (concurrent lanes) with FIFO and with the learned
              schedule (cost model trained on the committed cost records).
+large_d -- one run of the 100,000 x 25 workload (e2e, host buffers).
+real_shapes -- e2e ms per run on stand-ins with the sizes of the reference's
+             real-data runs and its real-data parameters, next to the wall
+             times the reference publishes for GPU-INSCY on the real datasets
+             (experiments/plot_real.py:14; other data, unstated hardware).
 
 `--impl reference` times the reference's CPU INSCY path (the oracle port of
 run_cpu3_weak) instead.  Multi-GPU: replicas only (`--gpus N` under torchrun
@@ -56,6 +61,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the label check against the oracle")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched / learned-schedule measurement")
+    ap.add_argument("--no-extra", action="store_true", help="skip the large_d and real-shape measurements")
     return ap.parse_args()
 
 
@@ -187,6 +193,42 @@ def batched_block(_lib):
             "labels_equal_plain": bool(same)}
 
 
+# GPU-INSCY wall times the reference publishes for its real datasets, in
+# seconds (experiments/plot_real.py:14); the shapes are synth.REAL_SHAPES
+REFERENCE_REAL_GPU_S = {"glass": 0.0615, "vowel": 0.0373, "pendigits": 3.037, "sky": 4.892}
+
+
+def extra_blocks(_lib):
+    """The 100,000 x 25 workload once, and the real-data shapes (e2e)."""
+    from gpu_inscy_gb300 import synth
+    out = {}
+    X = synth.make_large_d(0)
+    params = _lib.make_params(**synth.PARAMS["large_d"])
+    t0 = time.perf_counter()
+    subs, _, st = _lib.run_host(X, params)
+    t = time.perf_counter() - t0
+    out["large_d"] = {"workload": "large_d_n100000_d25 (seed 0)", "ms_per_run": 1000.0 * t,
+                      "points_per_s": X.shape[0] / t, "clustered_subspaces": len(subs),
+                      "subspaces_evaluated": int(st["subspaces"]), "candidates": int(st["candidates"]),
+                      "breakdown_ms": {k: st[k] for k in ("ms_expand", "ms_density", "ms_tree", "ms_cluster",
+                                                          "ms_replay", "ms_commit_tail", "ms_total")}}
+    shapes = {}
+    for name, (n, d, _) in synth.REAL_SHAPES.items():
+        X = synth.make_real_shape(name, seed=0)
+        params = _lib.make_params(**synth.real_params(n))
+        _lib.run_host(X, params)  # warm-up
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            subs, _, _ = _lib.run_host(X, params)
+            times.append(time.perf_counter() - t0)
+        shapes[name] = {"n": n, "d": d, "ms_per_run": 1000.0 * float(np.mean(times)),
+                        "clustered_subspaces": len(subs),
+                        "reference_gpu_inscy_s_on_the_real_dataset": REFERENCE_REAL_GPU_S[name]}
+    out["real_shapes"] = shapes
+    return out
+
+
 def run_reference(args, X, p):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -308,6 +350,8 @@ def main():
             "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_block(_lib)
+    if rank == 0 and not args.no_extra:
+        line.update(extra_blocks(_lib))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(X, p, args.cpu_sample)
     if rank == 0:

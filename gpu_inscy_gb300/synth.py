@@ -24,6 +24,12 @@ Workloads (with the INSCY parameters each one is run with):
 * ``huge``    n=1,000,000, d=32: 20 clusters with Zipf(1.5) sizes, std
   0.01-0.05, 2-10 dim subspaces, 4 pairs of clusters sharing a subspace,
   30 % noise.  eps=0.015 num_obj=16 min_size=64 cells=6.
+* ``real shapes``  stand-ins with the sizes of the reference's real-data
+  runs (glass 214 x 9, vowel 990 x 10, pendigits 7,494 x 16, sky 7,300 x 17):
+  Gaussian clusters (std 0.01-0.04) in 2-6 dim subspaces, 20 % noise, run with
+  the reference's real-data parameters (cells=4, num_obj=8, F=1, r=1,
+  min_size=0.05 n, eps=0.01, rectangular density).  The real datasets
+  themselves are not used.
 """
 import numpy as np
 
@@ -108,6 +114,28 @@ def make_huge(seed=0, n=1_000_000, d=32, n_clusters=20, noise_frac=0.30):
     subs = [np.sort(rng.choice(d, size=int(rng.integers(2, 11)), replace=False)) for _ in range(n_clusters)]
     for a in range(4):  # 4 pairs of clusters share a subspace
         subs[2 * a + 1] = subs[2 * a]
+    return subspace_clusters(rng, n, d, sizes, stds, subs)
+
+
+# name -> (n, d, clusters): the shapes of the reference's real-data runs
+REAL_SHAPES = {"glass": (214, 9, 6), "vowel": (990, 10, 11), "pendigits": (7494, 16, 10), "sky": (7300, 17, 8)}
+
+
+def real_params(n):
+    """The reference's real-data run parameters for n points."""
+    return dict(neighborhood_size=0.01, F=1.0, num_obj=8, min_size=int(0.05 * n), r=1.0, number_of_cells=4,
+                rectangular=True)
+
+
+def make_real_shape(name, seed=0):
+    n, d, k = REAL_SHAPES[name]
+    rng = np.random.default_rng(seed)
+    n_noise = n // 5
+    per = (n - n_noise) // k
+    sizes = [per] * k
+    sizes[-1] += n - n_noise - sum(sizes)
+    stds = rng.uniform(0.01, 0.04, size=k)
+    subs = [np.sort(rng.choice(d, size=int(rng.integers(2, min(d, 6) + 1)), replace=False)) for _ in range(k)]
     return subspace_clusters(rng, n, d, sizes, stds, subs)
 
 

@@ -39,6 +39,12 @@ def wide_cases():
     return family_cases("wide.npz")
 
 
+def real_shape_cases():
+    """glass, vowel, pendigits, sky shapes with the real-data parameters,
+    made by tests/golden/make_real_shapes.py."""
+    return family_cases("real_shapes.npz")
+
+
 def assert_same(got, want, what=""):
     gs, gl = got
     ws, wl = want

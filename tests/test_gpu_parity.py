@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as orc
-from golden_io import assert_same, family_cases, small_case, wide_cases
+from golden_io import assert_same, family_cases, real_shape_cases, small_case, wide_cases
 from gpu_inscy_gb300 import _lib, synth
 
 pytestmark = pytest.mark.gpu
@@ -43,6 +43,14 @@ def test_wide_rows_match_oracle_fixtures(engine, case):
     i, X, p, want = wide_cases()[case]
     got, _ = gpu_run(X, **p)
     assert_same(got, want, "wide %d (d=%d)" % (i, X.shape[1]))
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_real_shapes_match_oracle_fixtures(engine, case):
+    # the sizes and parameters of the reference's real-data runs (rectangular)
+    i, X, p, want = real_shape_cases()[case]
+    got, _ = gpu_run(X, **p)
+    assert_same(got, want, "real shape %d (n=%d, d=%d)" % (i, X.shape[0], X.shape[1]))
 
 
 def _random_case(seed):

@@ -15,7 +15,7 @@ import sys
 import numpy as np
 import pytest
 
-from golden_io import assert_same, family_cases, small_case, wide_cases
+from golden_io import assert_same, family_cases, real_shape_cases, small_case, wide_cases
 from gpu_inscy_gb300 import synth
 import oracle as orc
 
@@ -73,6 +73,12 @@ def test_wide_rows(driver):
     # d = 20: the density pass on 32-slot point rows
     i, X, p, want = wide_cases()[0]
     assert_same(simt_run(driver, X, p, True, "wide0"), want, "wide %d (d=%d)" % (i, X.shape[1]))
+
+
+def test_real_shapes_small(driver):
+    # glass and vowel shapes, real-data parameters (rectangular density)
+    for i, X, p, want in real_shape_cases()[:2]:
+        assert_same(simt_run(driver, X, p, i % 2 == 1, "real%d" % i), want, "real shape %d" % i)
 
 
 @pytest.fixture(scope="module")
