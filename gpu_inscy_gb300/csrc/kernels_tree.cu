@@ -174,6 +174,7 @@ struct TreeShared {
   long long goff;
   int gcount;
   int gwrite;
+  int gneed;  // detached chains undecided before the chains' sort
 };
 
 // leaf key of point x: its cells on the remaining dims (in level order, most
@@ -378,10 +379,12 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
           if (SV[j + 1] != SV[j]) a.out_pts[pts_off + SV[j]] = x;
         }
       }
-      // 6. ghosts of the pruned tree.  The region's detached chains (those
-      //    lying in the run, not starting on D) are sorted by the leaf key of
-      //    their points, so "does a deeper chain pass this node" is a range
-      //    search too.
+      // 6. ghosts of the pruned tree.  A detached chain's fate mostly follows
+      //    from the points' nodes (range searches on the sorted point keys);
+      //    only a chain whose sibling node holds no point at all needs "does
+      //    a deeper chain pass this node", a range search on the chains' own
+      //    keys, so the region's chains are sorted by leaf key only when
+      //    some chain needs that.
       int ngp = 0;
       if (ng > 0 && !drop) {
         for (int c = 0; c < ng; c += blockDim.x) {
@@ -400,28 +403,6 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
         __syncthreads();
         for (int j = threadIdx.x; j < ngp; j += blockDim.x) KG[j] = leaf_key<Key>(a.cc, d, s.lam, nlam, D, b, Gh[GA[j]].x);
         __syncthreads();
-        if (ngp > 1) {
-          Key* kc = KG;
-          Key* ko = KH;
-          int* gc = GA;
-          int* go = GB;
-          for (int sh = 0; sh < key_bits; sh += 8) {
-            block_sort_pass<kThreads / 32>(kc, gc, ko, go, ngp, sh, s.base, s.tot, s.wc);
-            Key* tk = kc;
-            kc = ko;
-            ko = tk;
-            int* t = gc;
-            gc = go;
-            go = t;
-          }
-          if (gc != GA) {
-            for (int j = threadIdx.x; j < ngp; j += blockDim.x) {
-              GA[j] = gc[j];
-              KG[j] = kc[j];
-            }
-            __syncthreads();
-          }
-        }
       }
       // The keep decisions are made once and stored in buffers free by now
       // (the key buffer the merge sort did not end in; the chains' sort
@@ -431,6 +412,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       if (threadIdx.x == 0) {
         s.gcount = 0;
         s.gwrite = 0;
+        s.gneed = 0;
       }
       __syncthreads();
       // (a) chains of points pruned here: a chain survives when a kept point
@@ -451,37 +433,65 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
         }
         kmask[j] = km;
       }
-      // (b) chains detached earlier
-      for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
+      // (b) chains detached earlier: 1 kept, 0 dropped, 2 undecided until the
+      //     chains are sorted (`sorted` false)
+      auto decide = [&](int jj, bool sorted) -> int {
         const int2 gg = Gh[GA[jj]];
         const int g = gg.y;
         const Key kx = KG[jj];
         const int l = __popcll(lammask & ((1ull << g) - 1));
         int plo, phi;
-        bool keep = true;
         if (l > 0) {
           key_range(kcur, m, kx, b * (nlam - l + 1), plo, phi);  // prefix through level l-1: the parent node
-          keep = SV[phi] - SV[plo] > 0;
+          if (SV[phi] - SV[plo] == 0) return 0;
         }
-        if (keep) {
-          key_range(kcur, m, kx, b * (nlam - l), plo, phi);
-          if (SV[phi] - SV[plo] > 0) {
-            keep = true;  // the sibling node keeps points
-          } else if (phi > plo) {
-            keep = false;  // the sibling node existed and is erased with it
-          } else {
-            // the sibling node exists only if a deeper detached chain passes it
-            int glo, ghi;
-            key_range(KG, ngp, kx, b * (nlam - l), glo, ghi);
-            for (int t = glo; t < ghi; ++t)
-              if (__popcll(lammask & ((1ull << Gh[GA[t]].y) - 1)) > l) {
-                keep = false;
-                break;
-              }
+        key_range(kcur, m, kx, b * (nlam - l), plo, phi);
+        if (SV[phi] - SV[plo] > 0) return 1;  // the sibling node keeps points
+        if (phi > plo) return 0;              // the sibling node existed and is erased with it
+        // the sibling node exists only if a deeper detached chain passes it
+        if (!sorted) return 2;
+        int glo, ghi;
+        key_range(KG, ngp, kx, b * (nlam - l), glo, ghi);
+        for (int t = glo; t < ghi; ++t)
+          if (__popcll(lammask & ((1ull << Gh[GA[t]].y) - 1)) > l) return 0;
+        return 1;
+      };
+      for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
+        const int k = decide(jj, ngp <= 1);
+        gkeep[jj] = k;
+        if (k == 2) atomicAdd(&s.gneed, 1);
+      }
+      __syncthreads();
+      if (s.gneed > 0) {
+        // sort the chains by leaf key (the sort buffers hold no decision yet
+        // worth keeping: all are made again on the sorted order)
+        Key* kc = KG;
+        Key* ko = KH;
+        int* gc = GA;
+        int* go = GB;
+        for (int sh = 0; sh < key_bits; sh += 8) {
+          block_sort_pass<kThreads / 32>(kc, gc, ko, go, ngp, sh, s.base, s.tot, s.wc);
+          Key* tk = kc;
+          kc = ko;
+          ko = tk;
+          int* t = gc;
+          gc = go;
+          go = t;
+        }
+        if (gc != GA) {
+          for (int j = threadIdx.x; j < ngp; j += blockDim.x) {
+            GA[j] = gc[j];
+            KG[j] = kc[j];
           }
+          __syncthreads();
         }
-        gkeep[jj] = keep ? 1 : 0;
-        if (keep) atomicAdd(&s.gcount, 1);
+        for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) gkeep[jj] = decide(jj, true);
+        __syncthreads();
+      }
+      {
+        int kept = 0;
+        for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) kept += gkeep[jj];
+        if (kept) atomicAdd(&s.gcount, kept);
       }
       __syncthreads();
       if (threadIdx.x == 0) {
