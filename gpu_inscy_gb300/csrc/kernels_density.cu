@@ -361,8 +361,11 @@ constexpr int kRowsSMs = 152;
 // resident blocks per SM: 64 registers a thread for 16-slot rows, 80 for 32
 constexpr int rows_blocks_per_sm(int slots) { return slots == 16 ? 4 : 3; }
 
-template <bool kWrite, int kS>
+// kMode: 0 count, 1 write at the counted offsets (loff), 2 single-pass write
+// at capacity offsets (cap_base)
+template <int kMode, int kS>
 __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows(DensityArgs a) {
+  constexpr bool kWrite = kMode >= 1;
   constexpr int kQ = kS / 4;           // 16-byte quarters of a row
   constexpr bool kPre = kS == 16;      // rows of the next chunk held in registers
   __shared__ float4 squery[8][kS];     // per warp and dim: the query's (x, lo, hi, -)
@@ -372,7 +375,7 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
   __shared__ unsigned long long sstat[8][3];
   const unsigned lane = lane_id();
   const int wb = (int)(threadIdx.x >> 5);
-  const bool single = kWrite && a.cap_base != nullptr;
+  constexpr bool single = kMode == 2;
   const float4* xrow4 = reinterpret_cast<const float4*>(a.xrow);
   const float4* qv = squery[wb];
   if (lane == 0) sstat[wb][0] = sstat[wb][1] = sstat[wb][2] = 0;  // lane 0 alone touches them
@@ -394,7 +397,11 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
       int run = 0;  // lane c: entries of child c so far
       long long ob = 0;
       if (single) {
-        ob = a.cap_base[w] + (long long)lane * len;
+        // child c writes at most len entries from cap_base[w] + c * len, so
+        // one check of the pair's block bounds every write below
+        const long long cb = a.cap_base[w];
+        if (!GUARD_OK(a.guard, cb >= 0 && cb + (long long)nc * len <= a.total, 39, cb)) continue;
+        ob = cb + (long long)lane * len;
       } else if (kWrite) {
         if ((int)lane < nc) ob = a.loff[item_c];
       }
@@ -470,7 +477,7 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
             const long long base = __shfl_sync(0xffffffffu, ob + run, c);
             if (ok) {
               const long long o = base + __popc(m & lanemask_lt());
-              if (GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) {
+              if (single || GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) {
                 a.lids[o] = q;
                 a.lacc[o] = acc2;
               }
@@ -996,16 +1003,21 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
     a.chunk = (int)(chunk < 1 ? 1 : chunk > 8 ? 8 : chunk);
     const long long need = (nwarps + 7) / 8;
     const unsigned blocks = (unsigned)(need < max_blocks ? need : max_blocks);
+    const int mode = write ? (L.cap_base ? 2 : 1) : 0;
     if (L.slots == 16) {
-      if (write)
-        k_neighbours_rows<true, 16><<<blocks, 256, 0, s>>>(a);
+      if (mode == 2)
+        k_neighbours_rows<2, 16><<<blocks, 256, 0, s>>>(a);
+      else if (mode == 1)
+        k_neighbours_rows<1, 16><<<blocks, 256, 0, s>>>(a);
       else
-        k_neighbours_rows<false, 16><<<blocks, 256, 0, s>>>(a);
+        k_neighbours_rows<0, 16><<<blocks, 256, 0, s>>>(a);
     } else {
-      if (write)
-        k_neighbours_rows<true, 32><<<blocks, 256, 0, s>>>(a);
+      if (mode == 2)
+        k_neighbours_rows<2, 32><<<blocks, 256, 0, s>>>(a);
+      else if (mode == 1)
+        k_neighbours_rows<1, 32><<<blocks, 256, 0, s>>>(a);
       else
-        k_neighbours_rows<false, 32><<<blocks, 256, 0, s>>>(a);
+        k_neighbours_rows<0, 32><<<blocks, 256, 0, s>>>(a);
     }
     return;
   }
