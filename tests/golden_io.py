@@ -35,7 +35,8 @@ def family_cases(name="family.npz"):
 
 
 def wide_cases():
-    """16 < d <= 32 (32-slot point rows), made by tests/golden/make_wide.py."""
+    """d = 17 .. 40 (32-slot point rows; the general density kernel and 128-bit
+    leaf keys above d = 32), made by tests/golden/make_wide.py."""
     return family_cases("wide.npz")
 
 

@@ -37,9 +37,10 @@ def test_family_matches_reference_outputs(engine, case):
     assert_same(got, want, "family %d" % i)
 
 
-@pytest.mark.parametrize("case", range(4))
+@pytest.mark.parametrize("case", range(6))
 def test_wide_rows_match_oracle_fixtures(engine, case):
-    # 16 < d <= 32: the density pass runs on 32-slot point rows
+    # 16 < d <= 32: the density pass runs on 32-slot point rows; d = 36, 40:
+    # the general density kernel and 128-bit leaf keys at the first levels
     i, X, p, want = wide_cases()[case]
     got, _ = gpu_run(X, **p)
     assert_same(got, want, "wide %d (d=%d)" % (i, X.shape[1]))

@@ -70,9 +70,10 @@ def test_family_cases(driver):
 
 
 def test_wide_rows(driver):
-    # d = 20: the density pass on 32-slot point rows
-    i, X, p, want = wide_cases()[0]
-    assert_same(simt_run(driver, X, p, True, "wide0"), want, "wide %d (d=%d)" % (i, X.shape[1]))
+    # d = 20: the density pass on 32-slot point rows; d = 36: the general
+    # density kernel and 128-bit leaf keys
+    for i, X, p, want in (wide_cases()[0], wide_cases()[4]):
+        assert_same(simt_run(driver, X, p, True, "wide%d" % i), want, "wide %d (d=%d)" % (i, X.shape[1]))
 
 
 def test_real_shapes_small(driver):
