@@ -1591,14 +1591,22 @@ bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
     Entry& E = *ents_[i];
     int mn = -1;
     if (!use_bits) {
-      rc_[7] += m;
-      for (int j = 0; j < m; ++j) {
-        int l = E.lab[pts[j]];
+      // the entry matters only if its minimum ends above max_min, so the scan
+      // stops once the minimum so far is at or below it
+      const int* lab = E.lab.data();
+      const int* esz = E.size.data();
+      int j = 0;
+      for (; j < m; ++j) {
+        const int l = lab[pts[j]];
         if (l >= 0) {
-          int v = E.size[l];
-          if (mn == -1 || v < mn) mn = v;
+          const int v = esz[l];
+          if (mn == -1 || v < mn) {
+            mn = v;
+            if (mn <= max_min) break;
+          }
         }
       }
+      rc_[7] += j < m ? j + 1 : m;
     } else {
       if (!bits_set) {
         for (int j = 0; j < m; ++j) tbits_[pts[j] >> 6] |= 1ull << (pts[j] & 63);
