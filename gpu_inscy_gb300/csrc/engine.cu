@@ -1262,16 +1262,17 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         int* comp = lv.get<int>(K + 1);
         int* root_of = lv.get<int>(K + 1);
         int* dsample = lv.get<int>(ncl + 1);
+        uint8_t* ddom = lv.get<uint8_t>(K + 1);  // per kept point: in its subspace's dominant component
         int* dnc = lv.get<int>(1);
         long long ncomp = 0;
         std::vector<int> cbase(nsubs + 1);
         stats_.ms_cluster += timed(s, [&] {
           launch_uf_init(CA.uf, K, s);
-          launch_uf_union(CA, ncl, dcslot, dsample, s);
+          launch_uf_union(CA, ncl, dcslot, dsample, ddom, s);
           launch_uf_flatten(CA, is_root, root_of, s);
           launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
         });
-        launches += 9;
+        launches += 10;
         ncomp = scalar(dnc, s);
         int* dcbase = lv.get<int>(nsubs + 1);
         launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);

@@ -159,7 +159,8 @@ struct ClusterArgs {
   Guard guard;
 };
 void launch_uf_init(int* par, long long n, cudaStream_t s);
-void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, cudaStream_t s);
+void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, uint8_t* dom,
+                     cudaStream_t s);
 void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s);
 void launch_comp_ids(const ClusterArgs& a, const int* root_id, const int* root_of, int* comp, int* mcount,
                      cudaStream_t s);

@@ -163,22 +163,37 @@ __global__ void k_uf_sample(ClusterArgs a, int nclustered, int* __restrict__ sam
   if (lane == 0) sample[cs] = best > 0 ? (int)win : -1;
 }
 
-// (3) one warp per kept point outside the dominant component: all its dense
-// neighbours; the point's own root is found once per 32 neighbours
-__global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const int* __restrict__ cslot_of,
-                                                  const int* __restrict__ sample) {
+// (2b) one thread per kept point: 1 when it is in its subspace's dominant
+// component (or is no dense point of a clustered subspace), else 0
+__global__ void __launch_bounds__(256) k_uf_dominant(ClusterArgs a, const int* __restrict__ cslot_of,
+                                                     const int* __restrict__ sample, uint8_t* __restrict__ dom) {
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  uint8_t f = 1;
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  if (a.clustered[si]) {
+    const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
+    if (bit_of(dn, a.keep_ids[kk])) {
+      const int smp = sample[cslot_of[si]];
+      f = (smp >= 0 && uf_find(a.uf, (int)kk) == uf_find(a.uf, smp)) ? 1 : 0;
+    }
+  }
+  dom[kk] = f;
+}
+
+// (3) one warp per dense point outside the dominant component (dom = 0): its
+// dense neighbours.  An edge between two such points is taken by the one with
+// the larger keep index (the other one's warp skips it; the neighbour relation
+// is symmetric), an edge to a dominant point always; edges between dominant
+// points join one component already.  The point's own root is found once per
+// 32 neighbours.
+__global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const uint8_t* __restrict__ dom) {
   const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (kk >= a.nkeep) return;
+  if (dom[kk]) return;
   const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
-  if (!a.clustered[si]) return;
   const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
-  const int p = a.keep_ids[kk];
-  if (!bit_of(dn, p)) return;
   const unsigned lane = lane_id();
-  const int smp = sample[cslot_of[si]];
-  int skip = 0;
-  if (lane == 0 && smp >= 0) skip = uf_find(a.uf, (int)kk) == uf_find(a.uf, smp);
-  if (__shfl_sync(0xffffffffu, skip, 0)) return;
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
   for (int j0 = 0; j0 < len; j0 += 32) {
@@ -188,7 +203,8 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const int* __re
       int q = a.lids[b + j];
       if (GUARD_OK(a.guard, q >= 0 && q < a.n, 61, q) && bit_of(dn, q)) {
         long long k2 = keep_index(a, si, q);
-        if (GUARD_OK(a.guard, k2 >= a.kstart[si] && k2 < a.kstart[si + 1], 62, k2)) kq = (int)k2;
+        if (GUARD_OK(a.guard, k2 >= a.kstart[si] && k2 < a.kstart[si + 1], 62, k2))
+          kq = (k2 < kk || dom[k2]) ? (int)k2 : -1;  // a larger non-dominant neighbour takes the edge
       }
     }
     if (!__any_sync(0xffffffffu, kq >= 0)) continue;
@@ -394,12 +410,14 @@ void launch_pack_order(const CallDesc* ncalls, int ncall, const int* order, cons
 void launch_uf_init(int* par, long long n, cudaStream_t s) {
   if (n > 0) k_uf_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(par, n);
 }
-void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, cudaStream_t s) {
+void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, uint8_t* dom,
+                     cudaStream_t s) {
   if (a.nkeep <= 0) return;
   k_uf_link2<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a);
   k_uf_compress<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a);
   if (nclustered > 0) k_uf_sample<<<(unsigned)((nclustered * 32LL + 255) / 256), 256, 0, s>>>(a, nclustered, sample);
-  k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a, cslot_of, sample);
+  k_uf_dominant<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, cslot_of, sample, dom);
+  k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a, dom);
 }
 void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s) {
   if (a.nkeep > 0) k_uf_flatten<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, is_root, root_of);
