@@ -238,27 +238,38 @@ __global__ void k_uf_flatten(ClusterArgs a, int* is_root, int* root_of) {
 }
 
 // component id (global, dense) of every dense kept point; -1 otherwise
+// atomicAdd(&ctr[key], 1) for every lane whose key is >= 0, with one atomic
+// per distinct key of the warp (large components put most lanes of a warp on
+// one counter); returns the lane's slot (the counter's old value + its rank
+// among the lanes with that key).  Every lane of the warp calls it.
+__device__ __forceinline__ int warp_inc(int* ctr, int key) {
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const int leader = __ffs((int)peers) - 1;
+  int base = 0;
+  if (key >= 0 && (int)lane_id() == leader) base = atomicAdd(&ctr[key], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return base + __popc(peers & lanemask_lt());
+}
+
 __global__ void k_comp_ids(ClusterArgs a, const int* __restrict__ root_id, const int* __restrict__ root_of,
                            int* __restrict__ comp, int* __restrict__ mcount) {
-  long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (kk >= a.nkeep) return;
-  int r = root_of[kk];
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = kk < a.nkeep;  // whole warps stay for warp_inc
   int c = -1;
-  if (r >= 0) {
-    c = root_id[r];
-    atomicAdd(&mcount[c], 1);
+  if (valid) {
+    const int r = root_of[kk];
+    if (r >= 0) c = root_id[r];
   }
-  comp[kk] = c;
+  warp_inc(mcount, c);
+  if (valid) comp[kk] = c;
 }
 
 __global__ void k_members(ClusterArgs a, const int* __restrict__ comp, const long long* __restrict__ moff,
                           int* __restrict__ mfill, int* __restrict__ members) {
-  long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (kk >= a.nkeep) return;
-  int c = comp[kk];
-  if (c < 0) return;
-  int o = atomicAdd(&mfill[c], 1);
-  members[moff[c] + o] = a.keep_ids[kk];
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = kk < a.nkeep ? comp[kk] : -1;  // whole warps stay for warp_inc
+  const int o = warp_inc(mfill, c);
+  if (c >= 0) members[moff[c] + o] = a.keep_ids[kk];
 }
 
 // border pairs (component, non-dense neighbour), de-duplicated through two
@@ -300,10 +311,8 @@ __global__ void __launch_bounds__(256) k_borders(ClusterArgs a, const int* __res
 }
 
 __global__ void k_border_count(const int* __restrict__ slots, long long nslots2, int* __restrict__ bcount) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nslots2) return;
-  int c = slots[i];
-  if (c >= 0) atomicAdd(&bcount[c], 1);
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  warp_inc(bcount, i < nslots2 ? slots[i] : -1);  // whole warps stay for warp_inc
 }
 
 __global__ void k_border_count_ovf(const int2* __restrict__ ovf, int novf, int* __restrict__ bcount) {
@@ -313,13 +322,10 @@ __global__ void k_border_count_ovf(const int2* __restrict__ ovf, int novf, int* 
 
 __global__ void k_border_fill(const int* __restrict__ slots, long long nslots2, int n, const long long* __restrict__ boff,
                               int* __restrict__ bfill, int* __restrict__ borders) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nslots2) return;
-  int c = slots[i];
-  if (c < 0) return;
-  int q = (int)((i >> 1) % n);
-  int o = atomicAdd(&bfill[c], 1);
-  borders[boff[c] + o] = q;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = i < nslots2 ? slots[i] : -1;  // whole warps stay for warp_inc
+  const int o = warp_inc(bfill, c);
+  if (c >= 0) borders[boff[c] + o] = (int)((i >> 1) % n);
 }
 
 __global__ void k_border_fill_ovf(const int2* __restrict__ ovf, int novf, const long long* __restrict__ boff,
