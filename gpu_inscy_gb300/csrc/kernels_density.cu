@@ -16,8 +16,12 @@
 // so a child adds exactly one term, in the reference's summation order.
 // Level-1 subspaces {D} read the precomputed candidate list of p's fine cell.
 //
-// One warp per (subspace, query point); candidates are consumed 32 at a time
-// with a ballot, and phi is accumulated over the accepted lanes in order.
+// Kernels: the candidate pass writes every item's ordered list (level 1:
+// k_neighbours, one warp per (subspace, query point); levels >= 2:
+// k_neighbours_rows over point rows when d <= 32, else k_neighbours_multi, one
+// warp per (parent subspace, query point) testing all children), candidates
+// 32 at a time with a ballot; k_density_phi then sums each list on one lane
+// and k_density_flags turns the sums into flags and bitmap bits.
 #include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -344,8 +348,8 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 //   * every candidate's row of coordinates (kS floats; the 16-byte quarters
 //     below the first child's dim are skipped) loaded once into registers,
 //     and the children walked by a loop over the kS dims unrolled at compile
-//     time (a group's children extend the parent by the
-//     consecutive dims d0 .. d0 + nc - 1, child c = dim d0 + c), so a
+//     time (a group's children extend the parent by the consecutive dims
+//     d0 .. d0 + nc - 1, child c = dim d0 + c), so a
 //     (candidate, child) test reads registers and one warp-uniform 16-byte
 //     shared load (the query's coordinate and fine-cell window on that dim).
 //     The +-1 fine-cell test is the equivalent interval test
@@ -356,7 +360,9 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 //     chunk k is tested;
 //   * warps taking `chunk` (group, query) pairs at a time from a work counter,
 //     so a warp whose list was short takes the next pair instead of idling
-//     until the longest list of its block is done.
+//     until the longest list of its block is done;
+//   * in the single pass, one bounds check per (group, query) block: child c
+//     writes at most len entries from its block's start.
 constexpr int kRowsSMs = 152;
 // resident blocks per SM: 64 registers a thread for 16-slot rows, 80 for 32
 constexpr int rows_blocks_per_sm(int slots) { return slots == 16 ? 4 : 3; }
