@@ -633,7 +633,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   };
   launch_prep(dX, ni, d, cells, csz, G, fsz, hp.eps, dcc, dfc, dgz, s);
   ++launches;
-  // point rows for the density pass when a row fits 16 or 32 slots
+  // point rows for the density pass when a row fits 16, 24 or 32 slots
   float* dxrow = nullptr;
   float* dwin = nullptr;
   unsigned long long* dwork = persist.get<unsigned long long>(1);

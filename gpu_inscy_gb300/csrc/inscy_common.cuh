@@ -23,8 +23,9 @@ namespace inscy {
 constexpr int kMaxDims = 64;    // subspaces are 64-bit masks
 constexpr int kMaxCells = 255;  // coarse cells fit a byte
 constexpr int kWarp = 32;
-// point rows of the density pass: 16 slots for d <= 16, 32 for d <= 32
-__host__ __device__ inline int row_slots(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : 0; }
+// point rows of the density pass: 16, 24 or 32 slots (the least >= d), none
+// above 32
+__host__ __device__ inline int row_slots(int d) { return d <= 16 ? 16 : d <= 24 ? 24 : d <= 32 ? 32 : 0; }
 
 // Region record written by the level kernel (one per restriction run).
 struct RegionRec {

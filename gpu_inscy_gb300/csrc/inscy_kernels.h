@@ -16,7 +16,7 @@ void launch_exclusive_scan_i2ll(const int* in, long long* out, long long n, long
 void launch_prep(const float* X, int n, int d, int cells, float csz, int G, float fsz, float eps, uint8_t* cc,
                  uint8_t* fc, unsigned long long* gz, cudaStream_t s);
 void launch_iota(int* a, int n, cudaStream_t s);
-// rows of `slots` (16 or 32 >= d) coordinates and fine-cell windows per point
+// rows of `slots` (16, 24 or 32 >= d) coordinates and fine-cell windows per point
 void launch_point_rows(const float* X, const uint8_t* fc, int n, int d, int slots, int G, const float* fine_lo,
                        float* xrow, float* win, cudaStream_t s);
 void launch_check_range(const float* X, long long m, int* bad, cudaStream_t s);
@@ -64,7 +64,7 @@ struct DensityLaunch {
   long long* cap_loff;              // single-pass write: list start of every item (out)
   const float* xrow;                // d <= 32: point rows (coordinates), else null
   const float* win;                 // d <= 32: fine-cell windows [lo, hi) per (point, dim)
-  int slots;                        // row width (16 or 32)
+  int slots;                        // row width (16, 24 or 32)
   unsigned long long* work;         // work counter of the row kernel (the caller zeroes it before each launch)
   RowItem* items;                   // row kernel: one record per (group, query), written by the capacity kernel
   unsigned long long* phi_work;     // scratch of the phi kernels (kPhiWorkBytes, zeroed by the caller before each launch)

@@ -78,7 +78,7 @@ struct DensityArgs {
   const float* win;
   unsigned long long* work;
   RowItem* items;        // per (group, query): written by k_list_capacity, read by k_neighbours_rows
-  int slots;             // row width of xrow / win (16 or 32; 0: no rows)
+  int slots;             // row width of xrow / win (16, 24 or 32; 0: no rows)
   int chunk;             // (group, query) pairs a warp takes per counter update
   long long prev_total;  // entries in the previous level's lists
   long long total;       // entries in this level's lists (write passes)
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
   }
 }
 
-// Levels >= 2 when d <= 32 (rows of kS = 16 or 32 slots): the same tests and
+// Levels >= 2 when d <= 32 (rows of kS = 16, 24 or 32 slots): the same tests and
 // outputs as k_neighbours_multi, with
 //   * the (group, query) pair read from its record (RowItem, resolved by
 //     k_list_capacity), so a pair starts after one load instead of a search
@@ -355,9 +355,9 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 //     The +-1 fine-cell test is the equivalent interval test
 //     lo_p <= x_q < hi_p, so no fine cell of the candidate is read;
 //   * a software pipeline over the 32-candidate chunks of a list: the ids and
-//     partial distances of chunk k + 2 and (kS = 16; 32-slot rows take too
-//     many registers to hold two) the rows of chunk k + 1 are loaded while
-//     chunk k is tested;
+//     partial distances of chunk k + 2 and (kS = 16, 24; 32-slot rows take
+//     too many registers to hold two) the rows of chunk k + 1 are loaded
+//     while chunk k is tested;
 //   * warps taking `chunk` (group, query) pairs at a time from a work counter,
 //     so a warp whose list was short takes the next pair instead of idling
 //     until the longest list of its block is done;
@@ -365,6 +365,8 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 //     writes at most len entries from its block's start.
 constexpr int kRowsSMs = 152;
 // resident blocks per SM: 64 registers a thread for 16-slot rows, 80 for 32
+// resident blocks per SM: 64 registers a thread for 16-slot rows, 85 for 24
+// and 32
 constexpr int rows_blocks_per_sm(int slots) { return slots == 16 ? 4 : 3; }
 
 // kMode: 0 count, 1 write at the counted offsets (loff), 2 single-pass write
@@ -373,7 +375,7 @@ template <int kMode, int kS>
 __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows(DensityArgs a) {
   constexpr bool kWrite = kMode >= 1;
   constexpr int kQ = kS / 4;           // 16-byte quarters of a row
-  constexpr bool kPre = kS == 16;      // rows of the next chunk held in registers
+  constexpr bool kPre = kS <= 24;      // rows of the next chunk held in registers
   __shared__ float4 squery[8][kS];     // per warp and dim: the query's (x, lo, hi, -)
   // per warp: candidate tests, list entries read, entries written; added to
   // the global counters once when the warp exits (per-pair atomics on three
@@ -1001,7 +1003,7 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
   if (nwarps <= 0) return;
   DensityArgs a = make_args(L);
   a.nwarps = nwarps;
-  if (L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 32) && L.d <= L.slots) {
+  if (L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 24 || L.slots == 32) && L.d <= L.slots) {
     // persistent warps: a grid that fills every SM once, (group, query) pairs
     // handed out by the work counter, several per update when there are many
     const long long max_blocks = (long long)kRowsSMs * rows_blocks_per_sm(L.slots);
@@ -1017,6 +1019,13 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
         k_neighbours_rows<1, 16><<<blocks, 256, 0, s>>>(a);
       else
         k_neighbours_rows<0, 16><<<blocks, 256, 0, s>>>(a);
+    } else if (L.slots == 24) {
+      if (mode == 2)
+        k_neighbours_rows<2, 24><<<blocks, 256, 0, s>>>(a);
+      else if (mode == 1)
+        k_neighbours_rows<1, 24><<<blocks, 256, 0, s>>>(a);
+      else
+        k_neighbours_rows<0, 24><<<blocks, 256, 0, s>>>(a);
     } else {
       if (mode == 2)
         k_neighbours_rows<2, 32><<<blocks, 256, 0, s>>>(a);

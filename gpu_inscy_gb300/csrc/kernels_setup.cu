@@ -128,7 +128,7 @@ void launch_prep(const float* X, int n, int d, int cells, float csz, int G, floa
   k_prep<<<(n + 255) / 256, 256, 0, s>>>(X, n, d, cells, csz, G, fsz, eps, cc, fc, gz);
 }
 
-// Point rows of `slots` (16 or 32) >= d: the coordinates of every point,
+// Point rows of `slots` (16, 24 or 32) >= d: the coordinates of every point,
 // zero-padded, and its fine-cell window per dim as a coordinate interval
 // [lo, hi) (fine_lo[k] = least x whose fine cell before the cap is >= k):
 // q is within +-1 fine cell of p on dim k iff lo_p <= x_q < hi_p.
