@@ -1266,13 +1266,40 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         int* dnc = lv.get<int>(1);
         long long ncomp = 0;
         std::vector<int> cbase(nsubs + 1);
-        stats_.ms_cluster += timed(s, [&] {
-          launch_uf_init(CA.uf, K, s);
-          launch_uf_union(CA, ncl, dcslot, dsample, ddom, s);
-          launch_uf_flatten(CA, is_root, root_of, s);
-          launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
-        });
-        launches += 10;
+        if (level == 1) {
+          // one-dim subspaces: components are runs in coordinate order
+          UfLevel1Scratch w;
+          w.flag = lv.get<int>(K + 1);
+          w.pos = lv.get<int>(K + 1);
+          w.total = lv.get<int>(1);
+          w.kidx = lv.get<int>(K + 1);
+          w.kbytes = lv.get<uint8_t>(5 * (K + 1));
+          w.perm0 = lv.get<int>(K + 1);
+          w.perm1 = lv.get<int>(K + 1);
+          w.hist = lv.get<int>(256 * ((K + kSortTile - 1) / kSortTile + 1));
+          w.start = lv.get<int>(K + 1);
+          w.runx = lv.get<int>(K + 1);
+          w.runmin = lv.get<int>(K + 1);
+          stats_.ms_cluster += timed(s, [&] {
+            launch_uf_init(CA.uf, K, s);
+            launch_uf_level1_count(CA, w, sums, s);
+          });
+          const int m = scalar(w.total, s);
+          stats_.ms_cluster += timed(s, [&] {
+            launch_uf_level1(CA, dX, d, dfc, acc_max, w, m, sums, s);
+            launch_uf_flatten(CA, is_root, root_of, s);
+            launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
+          });
+          launches += 40;
+        } else {
+          stats_.ms_cluster += timed(s, [&] {
+            launch_uf_init(CA.uf, K, s);
+            launch_uf_union(CA, ncl, dcslot, dsample, ddom, s);
+            launch_uf_flatten(CA, is_root, root_of, s);
+            launch_exclusive_scan_int(is_root, root_id, K, dnc, sums, s);
+          });
+          launches += 10;
+        }
         ncomp = scalar(dnc, s);
         int* dcbase = lv.get<int>(nsubs + 1);
         launch_gather_cbase(dkstart, nsubs, root_id, K, (int)ncomp, dcbase, s);

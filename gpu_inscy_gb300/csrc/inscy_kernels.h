@@ -161,6 +161,27 @@ struct ClusterArgs {
 void launch_uf_init(int* par, long long n, cudaStream_t s);
 void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, uint8_t* dom,
                      cudaStream_t s);
+// level 1 (one-dim subspaces): components as runs in coordinate order
+// instead of union-find (kept points K; element buffers of K; hist of
+// 256 * ceil(K / kSortTile) ints)
+struct UfLevel1Scratch {
+  int* flag;       // K
+  int* pos;        // K + 1
+  int* total;      // 1
+  int* kidx;       // K
+  uint8_t* kbytes; // 5 K
+  int* perm0;      // K
+  int* perm1;      // K
+  int* hist;
+  int* start;      // K
+  int* runx;       // K + 1
+  int* runmin;     // K
+};
+// first the dense points of clustered subspaces are counted (*w.total), then
+// with that count m the runs are found and the parents set
+void launch_uf_level1_count(const ClusterArgs& a, const UfLevel1Scratch& w, void* sums, cudaStream_t s);
+void launch_uf_level1(const ClusterArgs& a, const float* X, int d, const uint8_t* fc, float acc_max,
+                      const UfLevel1Scratch& w, int m, void* sums, cudaStream_t s);
 void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s);
 void launch_comp_ids(const ClusterArgs& a, const int* root_id, const int* root_of, int* comp, int* mcount,
                      cudaStream_t s);

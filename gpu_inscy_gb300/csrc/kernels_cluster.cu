@@ -218,6 +218,76 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const uint8_t* 
   }
 }
 
+// Level 1 (one-dim subspaces {D}): the neighbour relation on a line is
+// monotone -- for p <= q <= r in coordinate, p and r neighbours makes q a
+// neighbour of both (the +-1 fine-cell test and the distance only grow with
+// the gap) -- so the components of the dense points are the runs of
+// consecutive dense points, in coordinate order, whose consecutive pairs are
+// neighbours.  Every point's parent becomes the least keep index of its run,
+// the root union-find ends at (it hooks larger roots under smaller).
+
+// (1) dense points of clustered subspaces
+__global__ void k_l1_flags(ClusterArgs a, int* __restrict__ flag) {
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep) return;
+  int f = 0;
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  if (a.clustered[si]) f = bit_of(a.bitmaps + a.subs[si].bitmap_off + a.words, a.keep_ids[kk]) ? 1 : 0;
+  flag[kk] = f;
+}
+
+// (2) element e (compacted): its keep index and its sort key's bytes, least
+// significant first: the coordinate's bits (x >= 0: ordered as integers), then
+// the subspace
+__global__ void k_l1_pack(ClusterArgs a, const float* __restrict__ X, int d, const int* __restrict__ flag,
+                          const int* __restrict__ pos, int* __restrict__ kidx, uint8_t* __restrict__ kbytes) {
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= a.nkeep || !flag[kk]) return;
+  const int e = pos[kk];
+  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const unsigned u = __float_as_uint(X[(size_t)a.keep_ids[kk] * d + a.subs[si].dim]);
+  kidx[e] = (int)kk;
+  uint8_t* kb = kbytes + (size_t)e * 5;
+  kb[0] = (uint8_t)u;
+  kb[1] = (uint8_t)(u >> 8);
+  kb[2] = (uint8_t)(u >> 16);
+  kb[3] = (uint8_t)(u >> 24);
+  kb[4] = (uint8_t)si;
+}
+
+// (3) run starts in sorted order: not the same subspace as the previous
+// element, or not its neighbour
+__global__ void k_l1_starts(ClusterArgs a, const float* __restrict__ X, int d, const uint8_t* __restrict__ fc,
+                            float acc_max, const int* __restrict__ perm, const int* __restrict__ kidx, int m,
+                            int* __restrict__ start) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  int st = 1;
+  if (t > 0) {
+    const long long k1 = kidx[perm[t]], k0 = kidx[perm[t - 1]];
+    const int s1 = find_sub_by_keep(a.kstart, a.nsubs, k1), s0 = find_sub_by_keep(a.kstart, a.nsubs, k0);
+    if (s1 == s0) {
+      const int D = a.subs[s1].dim;
+      const size_t p = (size_t)a.keep_ids[k1] * d + D, q = (size_t)a.keep_ids[k0] * d + D;
+      const int fp = fc[p], fq = fc[q];
+      st = (fq >= fp - 1 && fq <= fp + 1 && dist_step(0.f, X[p], X[q]) <= acc_max) ? 0 : 1;
+    }
+  }
+  start[t] = st;
+}
+
+// (4) least keep index of every run, then every point's parent
+__global__ void k_l1_runmin(const int* __restrict__ perm, const int* __restrict__ kidx, const int* __restrict__ start,
+                            const int* __restrict__ runx, int m, int* __restrict__ runmin) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) atomicMin(&runmin[runx[t] + start[t] - 1], kidx[perm[t]]);
+}
+__global__ void k_l1_parent(const int* __restrict__ perm, const int* __restrict__ kidx, const int* __restrict__ start,
+                            const int* __restrict__ runx, int m, const int* __restrict__ runmin, int* __restrict__ par) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) par[kidx[perm[t]]] = runmin[runx[t] + start[t] - 1];
+}
+
 // roots: every dense point's root goes to a separate array (writing it into
 // `par` would race with the path-halving writes of concurrent finds, which
 // may store a non-root ancestor over it); roots are flagged
@@ -425,6 +495,34 @@ void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, 
   k_uf_dominant<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, cslot_of, sample, dom);
   k_uf_union<<<(unsigned)((a.nkeep * 32 + 255) / 256), 256, 0, s>>>(a, dom);
 }
+void launch_uf_level1_count(const ClusterArgs& a, const UfLevel1Scratch& w, void* sums, cudaStream_t s) {
+  if (a.nkeep <= 0) return;
+  k_l1_flags<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, w.flag);
+  launch_exclusive_scan_int(w.flag, w.pos, a.nkeep, w.total, sums, s);
+}
+
+void launch_uf_level1(const ClusterArgs& a, const float* X, int d, const uint8_t* fc, float acc_max,
+                      const UfLevel1Scratch& w, int m, void* sums, cudaStream_t s) {
+  if (a.nkeep <= 0 || m <= 0) return;
+  const unsigned kb = (unsigned)((a.nkeep + 255) / 256);
+  k_l1_pack<<<kb, 256, 0, s>>>(a, X, d, w.flag, w.pos, w.kidx, w.kbytes);
+  int* in = w.perm0;
+  int* out = w.perm1;
+  launch_iota(in, m, s);
+  for (int k = 0; k < 5; ++k) {  // LSD: coordinate bytes, then the subspace
+    launch_byte_sort_pass(in, out, m, w.kbytes, 5, k, w.hist, w.total, nullptr, sums, s);
+    int* t = in;
+    in = out;
+    out = t;
+  }
+  const unsigned mb = (unsigned)((m + 255) / 256);
+  k_l1_starts<<<mb, 256, 0, s>>>(a, X, d, fc, acc_max, in, w.kidx, m, w.start);
+  launch_exclusive_scan_int(w.start, w.runx, m, w.total, sums, s);
+  cudaMemsetAsync(w.runmin, 0x7f, sizeof(int) * (size_t)m, s);
+  k_l1_runmin<<<mb, 256, 0, s>>>(in, w.kidx, w.start, w.runx, m, w.runmin);
+  k_l1_parent<<<mb, 256, 0, s>>>(in, w.kidx, w.start, w.runx, m, w.runmin, a.uf);
+}
+
 void launch_uf_flatten(const ClusterArgs& a, int* is_root, int* root_of, cudaStream_t s) {
   if (a.nkeep > 0) k_uf_flatten<<<(unsigned)((a.nkeep + 255) / 256), 256, 0, s>>>(a, is_root, root_of);
 }
