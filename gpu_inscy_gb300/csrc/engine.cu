@@ -1256,6 +1256,12 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         CA.uf = lv.get<int>(K + 1);
         CA.err = derr;
         CA.guard = guard;
+        {
+          int* sub_of = lv.get<int>(K + 1);
+          launch_sub_of_keep(dkstart, nsubs, K, sub_of, s);
+          ++launches;
+          CA.sub_of = sub_of;
+        }
         CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
         int* is_root = lv.get<int>(K + 1);
         int* root_id = lv.get<int>(K + 1);

@@ -157,7 +157,9 @@ struct ClusterArgs {
   int* uf;
   int* err;
   Guard guard;
+  const int* sub_of;  // [nkeep] subspace of every kept point (launch_sub_of_keep)
 };
+void launch_sub_of_keep(const long long* kstart, int nsubs, long long nkeep, int* sub_of, cudaStream_t s);
 void launch_uf_init(int* par, long long n, cudaStream_t s);
 void launch_uf_union(const ClusterArgs& a, int nclustered, const int* cslot_of, int* sample, uint8_t* dom,
                      cudaStream_t s);

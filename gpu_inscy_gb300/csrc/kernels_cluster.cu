@@ -83,6 +83,17 @@ __device__ __forceinline__ void uf_unite(int* par, int ra, int rb, int* err) {
   }
 }
 
+// the subspace of every kept point (its kept index lies in the subspace's
+// range [kstart[si], kstart[si + 1])), looked up by the clustering kernels
+__global__ void k_sub_of_keep(const long long* __restrict__ kstart, int nsubs, long long nkeep, int* __restrict__ sub_of) {
+  const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk < nkeep) sub_of[kk] = find_sub_by_keep(kstart, nsubs, kk);
+}
+
+void launch_sub_of_keep(const long long* kstart, int nsubs, long long nkeep, int* sub_of, cudaStream_t s) {
+  if (nkeep > 0) k_sub_of_keep<<<(unsigned)((nkeep + 255) / 256), 256, 0, s>>>(kstart, nsubs, nkeep, sub_of);
+}
+
 __global__ void k_uf_init(int* par, long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) par[i] = (int)i;
@@ -101,7 +112,7 @@ __global__ void k_uf_init(int* par, long long n) {
 __global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
   const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   if (!a.clustered[si]) return;
   const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
   if (!bit_of(dn, a.keep_ids[kk])) return;
@@ -123,7 +134,7 @@ __global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
 __global__ void __launch_bounds__(256) k_uf_compress(ClusterArgs a) {
   const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   if (!a.clustered[si]) return;
   const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
   if (!bit_of(dn, a.keep_ids[kk])) return;
@@ -170,7 +181,7 @@ __global__ void __launch_bounds__(256) k_uf_dominant(ClusterArgs a, const int* _
   const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
   uint8_t f = 1;
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   if (a.clustered[si]) {
     const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
     if (bit_of(dn, a.keep_ids[kk])) {
@@ -191,7 +202,7 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const uint8_t* 
   const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (kk >= a.nkeep) return;
   if (dom[kk]) return;
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
   const unsigned lane = lane_id();
   const long long b = a.keep_loff[kk];
@@ -231,7 +242,7 @@ __global__ void k_l1_flags(ClusterArgs a, int* __restrict__ flag) {
   const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
   int f = 0;
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   if (a.clustered[si]) f = bit_of(a.bitmaps + a.subs[si].bitmap_off + a.words, a.keep_ids[kk]) ? 1 : 0;
   flag[kk] = f;
 }
@@ -244,7 +255,7 @@ __global__ void k_l1_pack(ClusterArgs a, const float* __restrict__ X, int d, con
   const long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep || !flag[kk]) return;
   const int e = pos[kk];
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   const unsigned u = __float_as_uint(X[(size_t)a.keep_ids[kk] * d + a.subs[si].dim]);
   kidx[e] = (int)kk;
   uint8_t* kb = kbytes + (size_t)e * 5;
@@ -265,7 +276,7 @@ __global__ void k_l1_starts(ClusterArgs a, const float* __restrict__ X, int d, c
   int st = 1;
   if (t > 0) {
     const long long k1 = kidx[perm[t]], k0 = kidx[perm[t - 1]];
-    const int s1 = find_sub_by_keep(a.kstart, a.nsubs, k1), s0 = find_sub_by_keep(a.kstart, a.nsubs, k0);
+    const int s1 = a.sub_of[k1], s0 = a.sub_of[k0];
     if (s1 == s0) {
       const int D = a.subs[s1].dim;
       const size_t p = (size_t)a.keep_ids[k1] * d + D, q = (size_t)a.keep_ids[k0] * d + D;
@@ -294,7 +305,7 @@ __global__ void k_l1_parent(const int* __restrict__ perm, const int* __restrict_
 __global__ void k_uf_flatten(ClusterArgs a, int* is_root, int* root_of) {
   long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= a.nkeep) return;
-  int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  int si = a.sub_of[kk];
   int root = 0, r = -1;
   if (a.clustered[si]) {
     const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
@@ -351,7 +362,7 @@ __global__ void __launch_bounds__(256) k_borders(ClusterArgs a, const int* __res
   if (kk >= a.nkeep) return;
   const int c = comp[kk];
   if (c < 0) return;
-  const int si = find_sub_by_keep(a.kstart, a.nsubs, kk);
+  const int si = a.sub_of[kk];
   const unsigned* dn = a.bitmaps + a.subs[si].bitmap_off + a.words;
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
