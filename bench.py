@@ -14,9 +14,14 @@ clustered per second (n / run time) and ms per run.
   roofline-- the density candidate pass (k_neighbours_rows, the dominant
              kernel; its level-1 counterpart is one of the averaged launches):
              algorithmic bytes per launch / its average launch time, against
-             the measured HBM copy bandwidth;
+             the measured HBM copy bandwidth; roofline_tree the same for the
+             restrict/merge/prune level kernel (k_tree_level);
+  parity  -- the timed run's labels against the oracle's on the same input
+             (tests/golden/full_plain.json: per-subspace label digests made by
+             the oracle restatement of the reference CPU INSCY);
   cpu_baseline -- the CPU restatement of the reference CPU INSCY (oracle/) on a
-             bounded sample of the workload, all host cores.
+             bounded sample of the workload (its first 8,000 rows), all host
+             cores.
 
 batched -- the 64-dataset batch workload: plain runs one after another vs the
              batched form (concurrent lanes) with FIFO and with the learned
@@ -28,8 +33,10 @@ real_shapes -- e2e ms per run on stand-ins with the sizes of the reference's
              (experiments/plot_real.py:14; other data, unstated hardware).
 
 `--impl reference` times the reference's CPU INSCY path (the oracle port of
-run_cpu3_weak) instead.  Multi-GPU: replicas only (`--gpus N` under torchrun
-runs N independent copies of the workload, one per GPU).
+run_cpu3_weak, all host cores) on the full workload instead: one complete run
+per step, as many steps (up to --steps) as fit in --ref-budget seconds.
+Multi-GPU: replicas only (`--gpus N` under torchrun runs N independent copies
+of the workload, one per GPU).
 """
 import argparse
 import json
@@ -57,9 +64,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--n", type=int, default=25_000, help="points (profiling captures use a smaller case)")
-    ap.add_argument("--cpu-sample", type=int, default=2000, help="rows of the workload the CPU baseline runs on")
+    ap.add_argument("--cpu-sample", type=int, default=8000, help="rows of the workload the CPU baseline runs on")
+    ap.add_argument("--ref-budget", type=float, default=240.0,
+                    help="--impl reference: seconds of timed CPU runs (at least one full run)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-check", action="store_true", help="skip the label check against the oracle")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched / learned-schedule measurement")
     ap.add_argument("--no-extra", action="store_true", help="skip the large_d and real-shape measurements")
     return ap.parse_args()
@@ -124,21 +132,35 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(X, p, sample_rows, steps=1):
-    """Oracle port of the reference CPU INSCY on the first `sample_rows` rows."""
+def cpu_baseline(X, p, sample_rows):
+    """Oracle port of the reference CPU INSCY on the first `sample_rows` rows
+    (one run, all host cores)."""
     import oracle as orc
     Xs = np.ascontiguousarray(X[:sample_rows])
     cores = os.cpu_count() or 1
     orc.load()
-    times = []
-    for _ in range(max(1, steps)):
-        t0 = time.perf_counter()
-        orc.run(Xs, **p, threads=cores)
-        times.append(time.perf_counter() - t0)
-    t = float(np.mean(times))
+    t0 = time.perf_counter()
+    orc.run(Xs, **p, threads=cores)
+    t = time.perf_counter() - t0
     return {"value": Xs.shape[0] / t, "unit": "points/s", "cores": cores, "kind": "port",
             "sample": "first %d of the %d rows of the %s workload, same parameters; %.2f s per run"
                       % (Xs.shape[0], X.shape[0], WORKLOAD, t)}
+
+
+def fixture_check(name, subs, labels, index=None):
+    """The CUDA path's output against an oracle fixture entry (True / False),
+    or None when the fixture does not exist."""
+    if os.path.join(ROOT, "tests") not in sys.path:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden_io import GOLDEN, full_fixture, result_digest
+    if not os.path.exists(os.path.join(GOLDEN, "full_%s.json" % name)):
+        return None
+    ents = full_fixture(name)["entries"]
+    e = ents[0] if index is None else next((x for x in ents if x.get("index") == index), None)
+    if e is None:
+        return None
+    g = result_digest(subs, labels)
+    return g["subspaces"] == e["subspaces"] and g["label_sha256"] == e["label_sha256"]
 
 
 def batched_block(_lib):
@@ -181,6 +203,12 @@ def batched_block(_lib):
     t_learned = time.perf_counter() - t0
     same = all(a[0] == b[0] and a[0] == c[0] and np.array_equal(np.asarray(a[1]), np.asarray(b[1])) and
                np.array_equal(np.asarray(a[1]), np.asarray(c[1])) for a, b, c in zip(plain, fifo, lrn))
+    # the datasets with oracle fixtures (tests/golden/full_batch.json)
+    checked = {}
+    for i in range(len(Xs)):
+        ok = fixture_check("batch", lrn[i][0], lrn[i][1], index=i)
+        if ok is not None:
+            checked[str(i)] = bool(ok)
     return {"workload": "batch64_seed0 (64 datasets, n log-uniform in [2000, 50000], d in [8, 20])",
             "datasets": len(Xs), "points": points, "lanes": lanes,
             "lanes_tried_s": {str(k): round(v, 3) for k, v in tried.items()},
@@ -190,7 +218,7 @@ def batched_block(_lib):
             "learned_vs_plain": sum(t_plain) / t_learned, "learned_vs_fifo": t_fifo / t_learned,
             "cost_model": {"records": len(recs), "median_abs_log_error": err,
                            "final_train_loss": float(model.loss_hist[-1])},
-            "labels_equal_plain": bool(same)}
+            "labels_equal_plain": bool(same), "labels_equal_oracle_fixtures": checked}
 
 
 # GPU-INSCY wall times the reference publishes for its real datasets, in
@@ -205,9 +233,10 @@ def extra_blocks(_lib):
     X = synth.make_large_d(0)
     params = _lib.make_params(**synth.PARAMS["large_d"])
     t0 = time.perf_counter()
-    subs, _, st = _lib.run_host(X, params)
+    subs, labs, st = _lib.run_host(X, params)
     t = time.perf_counter() - t0
     out["large_d"] = {"workload": "large_d_n100000_d25 (seed 0)", "ms_per_run": 1000.0 * t,
+                      "labels_equal_oracle_fixture": fixture_check("large_d", subs, labs),
                       "points_per_s": X.shape[0] / t, "clustered_subspaces": len(subs),
                       "subspaces_evaluated": int(st["subspaces"]), "candidates": int(st["candidates"]),
                       "breakdown_ms": {k: st[k] for k in ("ms_expand", "ms_density", "ms_tree", "ms_cluster",
@@ -230,17 +259,33 @@ def extra_blocks(_lib):
 
 
 def run_reference(args, X, p):
+    """The reference's CPU INSCY path (the oracle port of run_cpu3_weak, all
+    host cores) on the full workload: one complete run per step; steps stop
+    once --ref-budget seconds of runs are done (at least one).  A CPU run has
+    nothing to warm up beyond building the port, which happens first."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    cpu_baseline(X, p, args.cpu_sample, steps=max(1, min(args.warmup, 1)))  # warm-up (page-in, build)
-    res = cpu_baseline(X, p, args.cpu_sample, steps=args.steps)
-    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "points/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.cpu_sample / res["value"],
+    import oracle as orc
+    orc.load()
+    cores = os.cpu_count() or 1
+    times = []
+    while len(times) < max(1, args.steps):
+        t0 = time.perf_counter()
+        orc.run(X, **p, threads=cores)
+        times.append(time.perf_counter() - t0)
+        if sum(times) + times[-1] > args.ref_budget:
+            break
+    t = float(np.mean(times))
+    v = X.shape[0] / t
+    res = {"value": v, "unit": "points/s", "cores": cores, "kind": "port",
+           "sample": "the full %s workload (%d x %d), one complete run per step, %d step(s) in the %.0f s budget; "
+                     "%.2f s per run" % (WORKLOAD, X.shape[0], X.shape[1], len(times), args.ref_budget, t)}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
+            "steps": len(times), "warmup": 0, "ms_per_step": 1000.0 * t,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": int(X.shape[0]), "d": int(X.shape[1]), **p,
-                       "sample_rows": args.cpu_sample},
-            "cpu_baseline": res, "e2e": {"value": res["value"], "unit": "points/s", "h2d_bytes_per_step": 0,
+            "config": {"workload": WORKLOAD, "n": int(X.shape[0]), "d": int(X.shape[1]), **p, "seed": args.seed},
+            "cpu_baseline": res, "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0,
                                          "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -274,9 +319,6 @@ def main():
     for _ in range(args.warmup):
         subs, labels, stats = device_step()
     torch.cuda.synchronize()
-    ok = None
-    if not args.no_check:
-        import oracle as orc  # noqa: F401  (checker only)
     # ---- timed region (device-resident input)
     if ws > 1:
         torch.distributed.barrier()
@@ -330,8 +372,17 @@ def main():
             "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
             "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
-    # ---- label check against the oracle at a reduced size is done by the tests;
-    #      here the device and host entries must agree with each other
+    # the restrict/merge/prune level kernel: its algorithmic bytes over all
+    # levels / its device time per run
+    tree_gbs = st["tree_bytes"] / (st["ms_tree"] * 1e-3) / 1e9 if st["ms_tree"] > 0 else 0.0
+    roof_tree = {"bound": "hbm", "kernel": "k_tree_level (restrict / merge / prune)", "achieved": tree_gbs,
+                 "peak": peak, "unit": "GB/s", "frac": tree_gbs / peak, "peak_source": peak_kind,
+                 "bytes_per_run": st["tree_bytes"], "ms_per_run": st["ms_tree"]}
+    # ---- labels of the timed run against the oracle's (full-size fixture)
+    full = args.seed == 0 and n == 25_000
+    parity = {"fixture": "tests/golden/full_plain.json" if full else None,
+              "labels_bit_exact_vs_oracle": fixture_check("plain", subs, labels) if full else None,
+              "device_and_host_entries_agree": bool(same)}
     line = {"metric": METRIC, "value": ws * n / (ms * 1e-3), "unit": "points/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -340,14 +391,14 @@ def main():
             "e2e": {"value": ws * n / (e2e_ms * 1e-3), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": int(e2e_stats["h2d_bytes"]), "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"])},
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats_all)),
-            "roofline": roof, "clocks": clk,
+            "roofline": roof, "roofline_tree": roof_tree, "parity": parity, "clocks": clk,
             "breakdown_ms": {k: st[k] for k in ("ms_setup", "ms_density", "ms_density_pass1", "ms_tree",
                                                "ms_cluster", "ms_replay", "ms_replay_prune", "ms_replay_cluster",
                                                "ms_replay_join", "ms_d2h", "ms_expand", "ms_commit_tail",
                                                "ms_total")},
             "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
             "commit_counters": st["replay"],
-            "clustered_subspaces": len(subs), "device_and_host_entries_agree": bool(same)}
+            "clustered_subspaces": len(subs)}
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_block(_lib)
     if rank == 0 and not args.no_extra:

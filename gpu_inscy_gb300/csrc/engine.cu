@@ -426,6 +426,7 @@ class Engine {
  public:
   Engine() {
     CK(cudaGetDevice(&device_));
+    CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_));
     pool_.reset(new Pool(device_));
     {
       const int hw = (int)std::thread::hardware_concurrency();
@@ -494,6 +495,7 @@ class Engine {
   void split_pieces(long long work);
 
   int device_ = 0;
+  int sms_ = 1;  // SMs of the device (persistent grids fill each once)
   std::unique_ptr<Pool> pool_;
   Pinned pinned_;
   cudaEvent_t ev0_, ev1_;
@@ -914,6 +916,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.work = dxrow ? dwork : nullptr;
       DL.items = nullptr;
       DL.phi_work = dphiwork;
+      DL.sms = sms_;
       auto neighbours = [&](bool write) {
         if (level == 1) {
           launch_neighbours(DL, write, s);
@@ -1030,6 +1033,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       launches += 4;
       const long long K = scalar(dtot + 1, s);
       check_guard("density");
+      // kept (subspace, point) pairs are indexed by int in the clustering
+      // kernels (union-find parents, level-1 sort indices, member counts)
+      if (K >= (long long)INT_MAX)
+        throw Error(INSCY_ERR_LIMIT, "level " + std::to_string(level) + " keeps " + std::to_string(K) +
+                                         " (subspace, point) pairs; the limit is 2^31 - 2");
       int* keep_ids = keepmem->get<int>(K);
       long long* keep_loff = keepmem->get<long long>(K);
       int* keep_lcnt = keepmem->get<int>(K);
@@ -1158,7 +1166,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       recs.resize((size_t)nwork * cells);
       d2h(recs.data(), drecs, sizeof(RegionRec) * recs.size(), s);
       d2h(nrecs.data(), dnrecs, sizeof(int) * nwork, s);
-      stats_.tree_bytes += 0;
+      // algorithmic bytes of the level kernel: per (call, dim) work item and
+      // point of the call its id, its cell on the dim and its s-connection
+      // flags (4 + 1 + 8 B), per chain 8 B; per point and chain written 4 / 8 B
+      stats_.tree_bytes += 13.0 * (double)pts_cap + 8.0 * (double)ghost_in + 4.0 * (double)tops[0] +
+                           8.0 * (double)tops[1];
 
       // ---- 5. next level's calls (host records in the reference's order)
       std::vector<CallDesc> ncall;
@@ -1273,7 +1285,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         long long ncomp = 0;
         std::vector<int> cbase(nsubs + 1);
         if (level == 1) {
-          // one-dim subspaces: components are runs in coordinate order
+          // one-dim subspaces: components are runs in coordinate order.  The
+          // sort key holds the subspace in one byte: level 1 has d <= 64
+          // subspaces
+          if (nsubs > 256) throw Error(INSCY_ERR_INTERNAL, "level 1 has more than 256 subspaces");
           UfLevel1Scratch w;
           w.flag = lv.get<int>(K + 1);
           w.pos = lv.get<int>(K + 1);

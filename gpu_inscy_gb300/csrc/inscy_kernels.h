@@ -68,6 +68,7 @@ struct DensityLaunch {
   unsigned long long* work;         // work counter of the row kernel (the caller zeroes it before each launch)
   RowItem* items;                   // row kernel: one record per (group, query), written by the capacity kernel
   unsigned long long* phi_work;     // scratch of the phi kernels (kPhiWorkBytes, zeroed by the caller before each launch)
+  int sms;                          // SMs of the device: persistent grids fill each once
   long long prev_total;
   long long total;
   long long prev_nkeep;

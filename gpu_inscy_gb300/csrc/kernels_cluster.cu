@@ -263,7 +263,7 @@ __global__ void k_l1_pack(ClusterArgs a, const float* __restrict__ X, int d, con
   kb[1] = (uint8_t)(u >> 8);
   kb[2] = (uint8_t)(u >> 16);
   kb[3] = (uint8_t)(u >> 24);
-  kb[4] = (uint8_t)si;
+  kb[4] = (uint8_t)si;  // one byte: level 1 has d <= 64 subspaces (the engine checks nsubs <= 256)
 }
 
 // (3) run starts in sorted order: not the same subspace as the previous

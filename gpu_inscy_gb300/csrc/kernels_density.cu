@@ -363,8 +363,6 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 //     until the longest list of its block is done;
 //   * in the single pass, one bounds check per (group, query) block: child c
 //     writes at most len entries from its block's start.
-constexpr int kRowsSMs = 152;
-// resident blocks per SM: 64 registers a thread for 16-slot rows, 80 for 32
 // resident blocks per SM: 64 registers a thread for 16-slot rows, 85 for 24
 // and 32
 constexpr int rows_blocks_per_sm(int slots) { return slots == 16 ? 4 : 3; }
@@ -1006,7 +1004,7 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
   if (L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 24 || L.slots == 32) && L.d <= L.slots) {
     // persistent warps: a grid that fills every SM once, (group, query) pairs
     // handed out by the work counter, several per update when there are many
-    const long long max_blocks = (long long)kRowsSMs * rows_blocks_per_sm(L.slots);
+    const long long max_blocks = (long long)(L.sms > 0 ? L.sms : 1) * rows_blocks_per_sm(L.slots);
     long long chunk = nwarps / (max_blocks * 8 * 16);
     a.chunk = (int)(chunk < 1 ? 1 : chunk > 8 ? 8 : chunk);
     const long long need = (nwarps + 7) / 8;
@@ -1061,7 +1059,7 @@ void launch_density_flags(const DensityLaunch& L, float* phi, int* perm, cudaStr
     k_phi_class_starts<<<1, 32, 0, s>>>(hist, hist + kPhiClasses);
     k_phi_class_scatter<<<iblocks, 256, 0, s>>>(L.cnt, L.nitems, hist + kPhiClasses, perm);
     const long long need = (L.nitems + 255) / 256;  // one 32-item batch per warp
-    const long long cap = 152LL * kPhiBlocksPerSM;
+    const long long cap = (long long)(L.sms > 0 ? L.sms : 1) * kPhiBlocksPerSM;
     const unsigned blocks = (unsigned)(need < cap ? need : cap);
     k_density_phi<<<blocks, 256, 0, s>>>(a, perm, phi);
   }

@@ -12,6 +12,13 @@
 // process exits.  All calls share it: the counter is cleared at the start of
 // every call, and calls that overlap on the GPU (several streams or host
 // threads at once) race on it and may report each other's mismatches.
+//
+// The array's device address is looked up once per device and kept.  A
+// cudaDeviceReset loads the library's device code into a new context, where
+// the kept address is no longer the array's: a process that resets a device
+// must not call this entry on that device afterwards.  The kept address is
+// dropped whenever a CUDA call of the entry fails, so the next call looks it
+// up again.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -41,22 +48,31 @@ void* scratch_for(int dev) {
   return g_scratch_addr[dev];
 }
 
+// A CUDA call of the entry failed: forget the device's address.
+int64_t failed(int dev) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  g_scratch_addr[dev] = nullptr;
+  return INSCY_SELFTEST_NOALLOC_CUDA;
+}
+
 }  // namespace
 
 extern "C" int64_t inscy_selftest_noalloc(int64_t count, void* stream) {
   if (count < 0 || count > INSCY_SELFTEST_NOALLOC_MAX) return INSCY_SELFTEST_NOALLOC_TOO_LARGE;
+  // an error left pending by earlier work is the caller's: report it without
+  // clearing it, and launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return INSCY_SELFTEST_NOALLOC_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return INSCY_SELFTEST_NOALLOC_CUDA;
   void* scratch = scratch_for(dev);
-  if (!scratch) return INSCY_SELFTEST_NOALLOC_CUDA;
+  if (!scratch) return failed(dev);
   cudaStream_t s = (cudaStream_t)stream;
   unsigned long long* counter = (unsigned long long*)scratch;
-  if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) return INSCY_SELFTEST_NOALLOC_CUDA;
+  if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) return failed(dev);
   if (count > 0) inscy::launch_phi_selftest((unsigned long long)count, 0x5eedull, counter, s);
-  if (cudaGetLastError() != cudaSuccess) return INSCY_SELFTEST_NOALLOC_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return failed(dev);  // the launch's own error
   unsigned long long bad = 0;
-  if (cudaMemcpyAsync(&bad, counter, sizeof(bad), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    return INSCY_SELFTEST_NOALLOC_CUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return INSCY_SELFTEST_NOALLOC_CUDA;
+  if (cudaMemcpyAsync(&bad, counter, sizeof(bad), cudaMemcpyDeviceToHost, s) != cudaSuccess) return failed(dev);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return failed(dev);
   return (int64_t)bad;
 }

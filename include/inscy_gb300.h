@@ -165,8 +165,13 @@ int64_t inscy_selftest(int64_t count);
  * every GPU that loads it until exit).  The first call on a device looks up
  * the array's device address, so make that first call before any stream
  * capture.  Every call clears the counter; calls that overlap on the GPU
- * share it and race.  Same result as inscy_selftest(count) (work queued on
- * `stream`, a cudaStream_t or NULL).  count is limited to
+ * share it and race.  The looked-up address belongs to the device's current
+ * context: after a cudaDeviceReset of that device, do not call this entry on
+ * it again in the same process (the address is looked up anew only after a
+ * failed call).  An error already pending in the CUDA runtime when the entry
+ * is called is left in place and reported as INSCY_SELFTEST_NOALLOC_CUDA.
+ * Same result as inscy_selftest(count) (work queued on `stream`, a
+ * cudaStream_t or NULL).  count is limited to
  * INSCY_SELFTEST_NOALLOC_MAX; returns the mismatch count (0 expected),
  * INSCY_SELFTEST_NOALLOC_TOO_LARGE for count < 0 or above the limit, or
  * INSCY_SELFTEST_NOALLOC_CUDA when a CUDA call fails.  It does not touch

@@ -1,4 +1,6 @@
-"""Readers of the golden fixtures made by tests/golden/make_golden.py."""
+"""Readers of the golden fixtures made by the scripts in tests/golden/."""
+import hashlib
+import json
 import os
 
 import numpy as np
@@ -58,3 +60,42 @@ def assert_same(got, want, what=""):
         bad = np.flatnonzero(gl[i] != wl[i])
         assert bad.size == 0, "%s: labels of subspace %s differ at %d points (first %s: got %d want %d)" % (
             what, s, bad.size, bad[0], gl[i][bad[0]], wl[i][bad[0]])
+
+
+# --------------------------------------------------------------------------
+# Full-size fixtures (tests/golden/make_full.py): the oracle's output on the
+# timed workloads, stored as per-subspace digests of the label vectors.
+# --------------------------------------------------------------------------
+def array_digest(a):
+    """sha256 of an array's bytes (little-endian int32 / float32 as stored)."""
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def clusters_of(labels):
+    """Number of distinct cluster labels (>= 0), as count_number_of_clusters
+    counts them per subspace (python/inscy.py:88-107)."""
+    v = np.unique(np.asarray(labels))
+    return int((v >= 0).sum())
+
+
+def result_digest(subs, labels):
+    """labels: an int32 array [k, n] or a list of k int32 vectors."""
+    rows = [np.asarray(labels[i]).astype("<i4", copy=False) for i in range(len(subs))]
+    return {"subspaces": [list(map(int, s)) for s in subs],
+            "label_sha256": [array_digest(r) for r in rows],
+            "clusters": [clusters_of(r) for r in rows]}
+
+
+def full_fixture(name):
+    with open(os.path.join(GOLDEN, "full_%s.json" % name)) as f:
+        return json.load(f)
+
+
+def assert_digest(got_subs, got_labels, want, what=""):
+    """The CUDA path's result against a full-size fixture entry."""
+    g = result_digest(got_subs, got_labels)
+    assert g["subspaces"] == want["subspaces"], "%s: subspace lists differ (%d vs %d entries)" % (
+        what, len(g["subspaces"]), len(want["subspaces"]))
+    bad = [i for i, (a, b) in enumerate(zip(g["label_sha256"], want["label_sha256"])) if a != b]
+    assert not bad, "%s: labels of %d subspaces differ, first %s" % (what, len(bad), want["subspaces"][bad[0]])
+    assert g["clusters"] == want["clusters"]

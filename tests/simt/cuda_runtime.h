@@ -151,6 +151,7 @@ enum cudaMemcpyKind {
 enum { cudaMemAllocationTypePinned = 1 };
 enum { cudaMemLocationTypeDevice = 1 };
 enum cudaMemPoolAttr { cudaMemPoolAttrReleaseThreshold = 1 };
+enum cudaDeviceAttr { cudaDevAttrMultiProcessorCount = 16 };
 struct cudaMemLocation {
   int type, id;
 };
@@ -162,6 +163,7 @@ struct cudaMemPoolProps {
   unsigned char reserved[64];
 };
 cudaError_t cudaGetDevice(int* d);
+cudaError_t cudaDeviceGetAttribute(int* v, cudaDeviceAttr a, int device);
 const char* cudaGetErrorString(cudaError_t e);
 cudaError_t cudaGetLastError();
 cudaError_t cudaMemPoolCreate(cudaMemPool_t* p, const cudaMemPoolProps* props);

@@ -393,6 +393,12 @@ cudaError_t cudaGetDevice(int* d) {
   *d = 0;
   return cudaSuccess;
 }
+// the host stand-in reports a GB300's 152 SMs, so persistent grids have the
+// device's block count
+cudaError_t cudaDeviceGetAttribute(int* v, cudaDeviceAttr, int) {
+  *v = 152;
+  return cudaSuccess;
+}
 const char* cudaGetErrorString(cudaError_t e) { return e ? "simt error" : "no error"; }
 cudaError_t cudaGetLastError() { return cudaSuccess; }
 cudaError_t cudaMemPoolCreate(cudaMemPool_t* p, const cudaMemPoolProps*) {
