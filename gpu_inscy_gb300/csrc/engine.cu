@@ -669,9 +669,13 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     }
     float* dfine = persist.get<float>(G + 2);
     h2d(dfine, fine_lo.data(), sizeof(float) * (G + 2), s);
-    dxrow = persist.get<float>((size_t)n * slots);
+    // n rows and a sentinel row n whose coordinates are all 3.4e38 (bytes
+    // 0x7f): lanes past the end of a candidate list read it and, the square
+    // of their difference overflowing to +inf, pass no distance test
+    dxrow = persist.get<float>((size_t)(n + 1) * slots);
     dwin = persist.get<float>((size_t)n * slots * 2);
     launch_point_rows(dX, dfc, ni, d, slots, G, dfine, dxrow, dwin, s);
+    CK(cudaMemsetAsync(dxrow + (size_t)n * slots, 0x7f, sizeof(float) * slots, s));
     ++launches;
   }
   int* drank = persist.get<int>(n);
@@ -753,8 +757,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     int* keep_ids = nullptr;
     long long* keep_loff = nullptr;
     int* keep_lcnt = nullptr;
-    int* lids = nullptr;
-    float* lacc = nullptr;
+    int2* lent = nullptr;      // this level's list entries (ListEnt)
     long long prev_total = 0;  // list entries
     long long prev_nkeep = 0;  // kept points
   };
@@ -893,8 +896,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.prev_keep = F.keep_ids;
       DL.prev_loff = F.keep_loff;
       DL.prev_lcnt = F.keep_lcnt;
-      DL.prev_lids = F.lids;
-      DL.prev_lacc = F.lacc;
+      DL.prev_ent = F.lent;
       DL.cnt = dcnt;
       DL.flags = dflags;
       DL.bitmaps = dbm;
@@ -951,8 +953,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       long long* dtot = lv.get<long long>(2);
       void* sums = scan_sums(std::max(std::max(nitems, (long long)nsubs * W), ngroup_warps) + 1, s, lv);
       long long L = 0;
-      int* lids = nullptr;
-      float* lacc = nullptr;
+      int2* lent = nullptr;
       bool single = false;
       {
         // capacities: per (group, query) at levels >= 2, per item (the
@@ -972,12 +973,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         if (capt * 8 <= t_single_pass_bytes) {
           single = true;
           L = capt;
-          lids = keepmem->get<int>(L);
-          lacc = keepmem->get<float>(L);
+          lent = keepmem->get<int2>(L);
           DL.cap_base = cbase;
           DL.cap_loff = dloff;
-          DL.lids = lids;
-          DL.lacc = lacc;
+          DL.ent = lent;
           DL.total = L;
           const double ms1 = timed(s, [&] { neighbours(true); });
           stats_.ms_density += ms1;
@@ -1009,11 +1008,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         launch_exclusive_scan_i2ll(dcnt, dloff, nitems, dtot, sums, s);
         launches += 3;
         L = scalar(dtot, s);
-        lids = keepmem->get<int>(L);
-        lacc = keepmem->get<float>(L);
+        lent = keepmem->get<int2>(L);
         DL.loff = dloff;
-        DL.lids = lids;
-        DL.lacc = lacc;
+        DL.ent = lent;
         DL.total = L;
         float* dphi = lv.get<float>(nitems);
         int* dperm = lv.get<int>(nitems);
@@ -1257,7 +1254,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         CA.keep_ids = keep_ids;
         CA.keep_loff = keep_loff;
         CA.keep_lcnt = keep_lcnt;
-        CA.lids = lids;
+        CA.ent = lent;
         CA.bitmaps = dbm;
         CA.words = W;
         CA.keep_word_rank = dkwr;
@@ -1432,8 +1429,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       F.keep_ids = keep_ids;
       F.keep_loff = keep_loff;
       F.keep_lcnt = keep_lcnt;
-      F.lids = lids;
-      F.lacc = lacc;
+      F.lent = lent;
       F.prev_total = L;
       F.prev_nkeep = K;
       F.pts_total = (long long)tops[0];

@@ -28,6 +28,12 @@ void launch_candidate_lists(int n, int d, int G, const int* bucket_pts, const in
                             const uint8_t* fc, const long long* list_off, int* list_pts, cudaStream_t s);
 
 // ---- density (kernels_density.cu)
+// One entry of a neighbour list, 8 bytes: .x the neighbour's id, .y the bits
+// of the float sum of squared differences between query and neighbour over
+// the list's subspace (its dims in ascending order).  One load or store moves
+// a whole entry.
+using ListEnt = int2;
+
 struct DensityLaunch {
   const SubDesc* subs;
   int nsubs;
@@ -48,15 +54,13 @@ struct DensityLaunch {
   const int* prev_keep;
   const long long* prev_loff;
   const int* prev_lcnt;
-  const int* prev_lids;
-  const float* prev_lacc;
+  const int2* prev_ent;  // parent-level list entries (ListEnt)
   int* cnt;
   uint8_t* flags;
   unsigned* bitmaps;
   int words;
   const long long* loff;
-  int* lids;
-  float* lacc;
+  int2* ent;  // this level's list entries (ListEnt)
   unsigned long long* cand_counter;
   unsigned long long* list_counter;
   unsigned long long* out_counter;  // single-pass write: entries written
@@ -147,7 +151,7 @@ struct ClusterArgs {
   const int* keep_ids;
   const long long* keep_loff;
   const int* keep_lcnt;
-  const int* lids;
+  const int2* ent;  // list entries (ListEnt); .x is the neighbour
   const unsigned* bitmaps;
   int words;
   const int* keep_word_rank;  // [nsubs * words] global prefix of kept popcounts

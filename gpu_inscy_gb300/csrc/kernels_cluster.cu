@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
   const int len = a.keep_lcnt[kk];
   int linked = 0;
   for (int j = 0; j < len && linked < 2; ++j) {
-    int q = a.lids[b + j];
+    int q = a.ent[b + j].x;
     if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 63, q) || !bit_of(dn, q)) continue;
     long long kq = keep_index(a, si, q);
     if (!GUARD_OK(a.guard, kq >= a.kstart[si] && kq < a.kstart[si + 1], 64, kq)) continue;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const uint8_t* 
     const int j = j0 + (int)lane;
     int kq = -1;
     if (j < len) {
-      int q = a.lids[b + j];
+      int q = a.ent[b + j].x;
       if (GUARD_OK(a.guard, q >= 0 && q < a.n, 61, q) && bit_of(dn, q)) {
         long long k2 = keep_index(a, si, q);
         if (GUARD_OK(a.guard, k2 >= a.kstart[si] && k2 < a.kstart[si + 1], 62, k2))
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(256) k_borders(ClusterArgs a, const int* __res
   const int len = a.keep_lcnt[kk];
   int* sl = slots + (long long)cslot_of[si] * a.n * 2;
   for (int j = lane_id(); j < len; j += 32) {
-    int q = a.lids[b + j];
+    int q = a.ent[b + j].x;
     if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 65, q) || bit_of(dn, q)) continue;
     int* s2 = sl + 2LL * q;
     int v0 = ((volatile int*)s2)[0];

@@ -55,16 +55,14 @@ struct DensityArgs {
   const int* prev_keep;
   const long long* prev_loff;
   const int* prev_lcnt;
-  const int* prev_lids;
-  const float* prev_lacc;
+  const int2* prev_ent;  // parent-level list entries (ListEnt)
   // outputs
   int* cnt;           // [nitems] neighbours
   uint8_t* flags;     // [nitems]
   unsigned* bitmaps;  // per subspace 3 * W words (weak, dense, keep)
   int words;          // W = ceil(n / 32)
   const long long* loff;  // [nitems] list start of every item
-  int* lids;
-  float* lacc;
+  int2* ent;  // this level's list entries (ListEnt)
   unsigned long long* cand_counter;  // candidate tests (candidate x child subspace)
   unsigned long long* list_counter;  // list entries read
   unsigned long long* out_counter;   // list entries written (single-pass write)
@@ -167,8 +165,8 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
   if (!GUARD_OK(a.guard, p >= 0 && p < a.n, 22, p)) return;
   const float xp = a.X[(size_t)p * a.d + D];
   const int fp = a.fc[(size_t)p * a.d + D];
-  const int* ids;
-  const float* accs = nullptr;
+  const int* ids = nullptr;
+  const int2* ents = nullptr;
   long long len;
   if (level1) {
     long long b = a.cand_off[(size_t)D * a.G + fp], e = a.cand_off[(size_t)D * a.G + fp + 1];
@@ -176,8 +174,7 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     len = e - b;
   } else {
     long long b = a.prev_loff[S.query_off + i];
-    ids = a.prev_lids + b;
-    accs = a.prev_lacc + b;
+    ents = a.prev_ent + b;
     len = a.prev_lcnt[S.query_off + i];
     if (!GUARD_OK(a.guard, b >= 0 && len >= 0 && b + len <= a.prev_total, 23, b + len)) return;
   }
@@ -186,7 +183,8 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
   for (long long j0 = 0; j0 < len; j0 += 32) {
     long long j = j0 + lane;
     bool ok = j < len;
-    int q = ok ? ids[j] : -1;
+    const int2 e = ok && !level1 ? ents[j] : make_int2(-1, 0);
+    int q = ok ? (level1 ? ids[j] : e.x) : -1;
     if (ok && !GUARD_OK(a.guard, q >= 0 && q < a.n, 24, q)) ok = false;
     ok = ok && q != p;
     if (ok && !level1) {
@@ -195,17 +193,14 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     }
     float acc2 = 0.f;
     if (ok) {
-      float acc = level1 ? 0.f : accs[j];
+      float acc = level1 ? 0.f : __int_as_float(e.y);
       acc2 = dist_step(acc, xp, a.X[(size_t)q * a.d + D]);
       ok = acc2 <= a.acc_max;
     }
     unsigned m = __ballot_sync(0xffffffffu, ok);
     if (kWrite && ok) {
       long long o = wbase + count + __popc(m & lanemask_lt());
-      if (GUARD_OK(a.guard, o >= 0 && o < a.total, 25, o)) {
-        a.lids[o] = q;
-        a.lacc[o] = acc2;
-      }
+      if (GUARD_OK(a.guard, o >= 0 && o < a.total, 25, o)) a.ent[o] = make_int2(q, __float_as_int(acc2));
     }
     count += __popc(m);
   }
@@ -256,8 +251,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
   const int p = a.prev_keep[S0.query_off + i];
   if (!GUARD_OK(a.guard, p >= 0 && p < a.n, 32, p)) return;
   const long long pb = a.prev_loff[S0.query_off + i];
-  const int* ids = a.prev_lids + pb;
-  const float* accs = a.prev_lacc + pb;
+  const int2* ents = a.prev_ent + pb;
   const long long len = a.prev_lcnt[S0.query_off + i];
   if (!GUARD_OK(a.guard, pb >= 0 && len >= 0 && pb + len <= a.prev_total, 33, pb + len)) return;
   const float* xrow_p = a.X + (size_t)p * a.d;
@@ -274,8 +268,9 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
   for (long long j0 = 0; j0 < len; j0 += 32) {
     const long long j = j0 + lane;
     bool in = j < len;
-    int q = in ? ids[j] : p;
-    const float acc0 = in ? accs[j] : 0.f;  // loaded before the id check, which may store
+    const int2 e = in ? ents[j] : make_int2(p, 0);
+    int q = e.x;
+    const float acc0 = __int_as_float(e.y);  // read before the id check, which may store
     if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
       in = false;
       q = p;
@@ -300,10 +295,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
         long long base = __shfl_sync(0xffffffffu, c < 32 ? ob0 + run0 : ob1 + run1, owner);
         if (ok) {
           long long o = base + __popc(m & lanemask_lt());
-          if (GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) {
-            a.lids[o] = q;
-            a.lacc[o] = acc2;
-          }
+          if (GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) a.ent[o] = make_int2(q, __float_as_int(acc2));
         }
       }
       if ((int)lane == (c & 31)) {
@@ -380,10 +372,16 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
   // adjacent counters saturate one L2 slice)
   __shared__ unsigned long long sstat[8][3];
   const unsigned lane = lane_id();
+  const unsigned lt = lanemask_lt();  // read once: the lanes below this one
   const int wb = (int)(threadIdx.x >> 5);
   constexpr bool single = kMode == 2;
   const float4* xrow4 = reinterpret_cast<const float4*>(a.xrow);
   const float4* qv = squery[wb];
+  const float acc_max = a.acc_max;
+  // lanes past the end of a list load row n of xrow, whose coordinates are
+  // all 3.4e38: (x_p - 3.4e38)^2 overflows to +inf, so they pass no distance
+  // test and need no flag of their own
+  const int sentinel = a.n;
   if (lane == 0) sstat[wb][0] = sstat[wb][1] = sstat[wb][2] = 0;  // lane 0 alone touches them
   for (;;) {
     unsigned long long take = 0;
@@ -396,8 +394,7 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
       if (r.len < 0) continue;  // failed its checks (reported by the capacity kernel)
       const int p = r.p, nc = r.nc, D0 = r.d0;
       const long long len = r.len;
-      const int* ids = a.prev_lids + r.pb;
-      const float* accs = a.prev_lacc + r.pb;
+      const int2* ents = a.prev_ent + r.pb;
       // lane c: the work item of child c (read now, used after the list)
       const long long item_c = (int)lane < nc ? a.subs[r.sub_base + lane].item_off + r.i : 0;
       int run = 0;  // lane c: entries of child c so far
@@ -416,18 +413,20 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
         const size_t t = (size_t)p * kS + lane;
         squery[wb][lane] = make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
       }
-      // candidate j of the list (lanes past the end stand on the query
-      // itself); nothing reads the loaded values until load_row, a chunk later
+      // candidate j of the list, one 8-byte entry (lanes past the end stand
+      // on the sentinel row); nothing reads the loaded values until load_row,
+      // a chunk later
       auto fetch = [&](long long j, bool& in, int& q, float& acc) {
         in = j < len;
-        q = in ? ids[j] : p;
-        acc = in ? accs[j] : 0.f;
+        const int2 e = in ? ents[j] : make_int2(sentinel, 0);
+        q = e.x;
+        acc = __int_as_float(e.y);
       };
       // the id is checked where it is first used: the load of its row
       auto load_row = [&](float4 (&x)[kQ], bool& in, int& q) {
         if (in && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) {
           in = false;
-          q = p;
+          q = sentinel;
         }
 #pragma unroll
         for (int t = 0; t < kQ; ++t)
@@ -435,7 +434,7 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
       };
       const long long nchunks = (len + 31) >> 5;
       bool in_a = false, in_b = false;
-      int q_a = p, q_b = p;
+      int q_a = sentinel, q_b = sentinel;
       float acc_a = 0.f, acc_b = 0.f;
       float4 xa[kQ], xb[kQ];  // xb: the next chunk's rows (kPre only)
 #pragma unroll
@@ -453,7 +452,6 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
         } else {
           load_row(xa, in_a, q_a);
         }
-        const bool in = in_a;
         const int q = q_a;
         const float acc = acc_a;
         in_a = in_b;
@@ -468,7 +466,6 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
           xq[4 * t + 2] = xa[t].z;
           xq[4 * t + 3] = xa[t].w;
         }
-        const bool live = in && q != p;
 #pragma unroll
         for (int D = 0; D < kS; ++D) {
           const int c = D - D0;
@@ -476,17 +473,15 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
           const float4 v = qv[D];
           const float xd = xq[D];
           const float acc2 = dist_step(acc, v.x, xd);
-          const bool ok = live && xd >= v.y && xd < v.z && acc2 <= a.acc_max;
+          const bool ok = xd >= v.y && xd < v.z && acc2 <= acc_max;
           const unsigned m = __ballot_sync(0xffffffffu, ok);
           if (!m) continue;
           if (kWrite) {
             const long long base = __shfl_sync(0xffffffffu, ob + run, c);
             if (ok) {
-              const long long o = base + __popc(m & lanemask_lt());
-              if (single || GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o)) {
-                a.lids[o] = q;
-                a.lacc[o] = acc2;
-              }
+              const long long o = base + __popc(m & lt);
+              if (single || GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o))
+                a.ent[o] = make_int2(q, __float_as_int(acc2));
             }
           }
           if ((int)lane == c) run += __popc(m);
@@ -694,7 +689,7 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
     bpos = 0;
   };
   long long item = 0;
-  const float* acc = nullptr;
+  const int2* acc = nullptr;  // the item's list entries
   int c = 0, j = 0;
   float sum = 0.f;
   bool live = false;  // this lane holds an item whose sum is still to be stored
@@ -732,7 +727,7 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
       c = cur ? c0 : c1;
       const long long lo = cur ? l0 : l1;
       live = (cur ? v0 : v1) && GUARD_OK(a.guard, c >= 0 && lo >= 0 && lo + c <= a.total, 41, lo + c);
-      acc = a.lacc + lo;
+      acc = a.ent + lo;
       j = 0;
       sum = 0.f;
     }
@@ -748,10 +743,11 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
       // the terms do not depend on the sum: four at a time are loaded and
       // computed side by side, then added in order (the sum's chain alone is
       // sequential)
-      const float* ap = acc + j;
+      const int2* ap = acc + j;
       int t = 0;
       for (; t + 4 <= steps; t += 4) {
-        const float a0 = ap[t], a1 = ap[t + 1], a2 = ap[t + 2], a3 = ap[t + 3];
+        const float a0 = __int_as_float(ap[t].y), a1 = __int_as_float(ap[t + 1].y);
+        const float a2 = __int_as_float(ap[t + 2].y), a3 = __int_as_float(ap[t + 3].y);
         const float d0 = __fdiv_rn(__fsqrt_rn(a0), a.eps), d1 = __fdiv_rn(__fsqrt_rn(a1), a.eps);
         const float d2 = __fdiv_rn(__fsqrt_rn(a2), a.eps), d3 = __fdiv_rn(__fsqrt_rn(a3), a.eps);
         sum = phi_step_exact(sum, __fmul_rn(d0, d0));  // integer pipe, no FP64
@@ -760,7 +756,7 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
         sum = phi_step_exact(sum, __fmul_rn(d3, d3));
       }
       for (; t < steps; ++t) {
-        const float dd = __fdiv_rn(__fsqrt_rn(ap[t]), a.eps);
+        const float dd = __fdiv_rn(__fsqrt_rn(__int_as_float(ap[t].y)), a.eps);
         sum = phi_step_exact(sum, __fmul_rn(dd, dd));
       }
       j += steps;
@@ -925,15 +921,13 @@ static DensityArgs make_args(const DensityLaunch& L) {
   a.prev_keep = L.prev_keep;
   a.prev_loff = L.prev_loff;
   a.prev_lcnt = L.prev_lcnt;
-  a.prev_lids = L.prev_lids;
-  a.prev_lacc = L.prev_lacc;
+  a.prev_ent = L.prev_ent;
   a.cnt = L.cnt;
   a.flags = L.flags;
   a.bitmaps = L.bitmaps;
   a.words = L.words;
   a.loff = L.loff;
-  a.lids = L.lids;
-  a.lacc = L.lacc;
+  a.ent = L.ent;
   a.cand_counter = L.cand_counter;
   a.list_counter = L.list_counter;
   a.out_counter = L.out_counter;

@@ -109,6 +109,8 @@ inline double __dadd_rn(double a, double b) { return a + b; }
 inline float __double2float_rn(double a) { return (float)a; }
 inline float __uint_as_float(unsigned u) { return simt::from_bits<float>(u); }
 inline unsigned __float_as_uint(float f) { return (unsigned)simt::to_bits(f); }
+inline float __int_as_float(int i) { return simt::from_bits<float>((unsigned)i); }
+inline int __float_as_int(float f) { return (int)(unsigned)simt::to_bits(f); }
 
 // blocks run on several host threads: real atomics
 template <class T>
