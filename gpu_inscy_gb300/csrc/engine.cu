@@ -310,7 +310,10 @@ struct LoopState {
 
 // Host threads for the data-parallel loops of the commit.  run(tasks, fn)
 // calls fn(i) for every i in [0, tasks) on the workers and the calling
-// thread and returns when all are done.
+// thread and returns when all are done.  Only as many workers as there are
+// tasks beyond the caller's are woken, and the caller waits for the tasks,
+// not for every worker to check in (a late worker finds the run's counter
+// exhausted and calls nothing).
 class HostPool {
  public:
   explicit HostPool(int workers) {
@@ -327,49 +330,66 @@ class HostPool {
   }
   int workers() const { return (int)th_.size(); }
   void run(int tasks, const std::function<void(int)>& fn) {
-    {
-      std::lock_guard<std::mutex> g(m_);
-      fn_ = &fn;
-      tasks_ = tasks;
-      next_.store(0);
-      pending_ = (int)th_.size();
-      ++gen_;
+    if (tasks <= 0) return;
+    auto job = std::make_shared<Job>();
+    job->fn = &fn;
+    job->tasks = tasks;
+    const int wake = std::min(tasks - 1, (int)th_.size());
+    if (wake > 0) {
+      {
+        std::lock_guard<std::mutex> g(m_);
+        cur_ = job;
+        ++gen_;
+      }
+      if (wake == (int)th_.size())
+        cv_.notify_all();
+      else
+        for (int i = 0; i < wake; ++i) cv_.notify_one();
     }
-    cv_.notify_all();
-    work();
-    std::unique_lock<std::mutex> lk(m_);
-    done_.wait(lk, [&] { return pending_ == 0; });
-    fn_ = nullptr;
+    work(*job);
+    if (job->done.load(std::memory_order_acquire) < tasks) {
+      std::unique_lock<std::mutex> lk(m_);
+      done_.wait(lk, [&] { return job->done.load(std::memory_order_acquire) >= tasks; });
+    }
+    std::lock_guard<std::mutex> g(m_);
+    if (cur_ == job) cur_.reset();
   }
 
  private:
-  void work() {
+  struct Job {
+    const std::function<void(int)>* fn = nullptr;
+    int tasks = 0;
+    std::atomic<int> next{0}, done{0};
+  };
+  void work(Job& j) {
     for (;;) {
-      const int i = next_.fetch_add(1);
-      if (i >= tasks_) break;
-      (*fn_)(i);
+      const int i = j.next.fetch_add(1);
+      if (i >= j.tasks) break;
+      (*j.fn)(i);
+      if (j.done.fetch_add(1, std::memory_order_acq_rel) + 1 == j.tasks) {
+        std::lock_guard<std::mutex> g(m_);
+        done_.notify_all();
+      }
     }
   }
   void loop() {
     long long seen = 0;
     for (;;) {
+      std::shared_ptr<Job> job;
       {
         std::unique_lock<std::mutex> lk(m_);
         cv_.wait(lk, [&] { return gen_ != seen; });
         seen = gen_;
         if (stop_) return;
+        job = cur_;
       }
-      work();
-      std::lock_guard<std::mutex> g(m_);
-      if (--pending_ == 0) done_.notify_all();
+      if (job) work(*job);
     }
   }
   std::vector<std::thread> th_;
   std::mutex m_;
   std::condition_variable cv_, done_;
-  const std::function<void(int)>* fn_ = nullptr;
-  std::atomic<int> next_{0};
-  int tasks_ = 0, pending_ = 0;
+  std::shared_ptr<Job> cur_;
   long long gen_ = 0;
   bool stop_ = false;
 };
@@ -391,7 +411,16 @@ static bool walk_test(const Walk& w, const LoopVec& V, const int* size, float r,
   bool hit = false;
   const uint64_t* gv = V.gv.data();
   const uint64_t cur = V.cur;
+  // the two lookups of a point are random reads of n-long vectors (several
+  // superset entries per join: more than a core's L2 holds), so the points a
+  // few iterations ahead are prefetched
+  constexpr long long kAhead = 16;
   for (long long k = w.k0; k < w.k1; ++k) {
+    if (k + kAhead < w.k1) {
+      const int qa = w.mem[k + kAhead];
+      __builtin_prefetch(w.lab + qa);
+      __builtin_prefetch(gv + qa);
+    }
     const int q = w.mem[k];
     if (w.lab[q] != w.l) continue;
     const uint64_t x = gv[q];
@@ -430,7 +459,7 @@ class Engine {
     pool_.reset(new Pool(device_));
     {
       const int hw = (int)std::thread::hardware_concurrency();
-      hpool_.reset(new HostPool(t_pool_workers >= 0 ? t_pool_workers : std::max(0, std::min(7, hw / 2 - 1))));
+      hpool_.reset(new HostPool(t_pool_workers >= 0 ? t_pool_workers : std::max(0, std::min(15, hw - 2))));
     }
     CK(cudaEventCreate(&ev0_));
     CK(cudaEventCreate(&ev1_));
@@ -1923,19 +1952,28 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     split_pieces(work);
     hpool_->run((int)split_.size(), [&](int i) {
       const Walk& w = split_[i];
+      // the sizes of the labels overwritten, subtracted once per run of
+      // equal old labels (the points of a piece mostly share one)
+      int run_l = -1, run_n = 0;
+      auto drop = [&](int ov) {
+        if (ov < 0) return;
+        if (ov != run_l) {
+          if (run_n) __atomic_fetch_sub(&esz[run_l], run_n, __ATOMIC_RELAXED);
+          run_l = ov;
+          run_n = 0;
+        }
+        ++run_n;
+      };
       if (w.l >= 0) {
         for (long long k = w.k0; k < w.k1; ++k) {
           const int p = w.mem[k];
-          const int ov = lab[p];
-          if (ov >= 0) __atomic_fetch_sub(&esz[ov], 1, __ATOMIC_RELAXED);
+          drop(lab[p]);
           lab[p] = w.l;
         }
       } else {
-        for (long long k = w.k0; k < w.k1; ++k) {
-          const int ov = __atomic_exchange_n(&lab[w.mem[k]], -2, __ATOMIC_RELAXED);
-          if (ov >= 0) __atomic_fetch_sub(&esz[ov], 1, __ATOMIC_RELAXED);
-        }
+        for (long long k = w.k0; k < w.k1; ++k) drop(__atomic_exchange_n(&lab[w.mem[k]], -2, __ATOMIC_RELAXED));
       }
+      if (run_n) __atomic_fetch_sub(&esz[run_l], run_n, __ATOMIC_RELAXED);
     });
   }
   // v_max over the whole vector: the largest label that still has points,
