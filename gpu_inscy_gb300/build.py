@@ -5,6 +5,9 @@ then linked into gpu_inscy_gb300/libinscy_gb300.so.  Floating point is
 compiled without multiply-add contraction and with IEEE division and square
 root, because the density tests must round exactly as the reference's
 host code does.
+
+build_ext() then compiles the PyTorch binding (csrc/torch_binding.cpp, module
+inscy_gb300_ext) against that library, in-tree under _build/ext.
 """
 import concurrent.futures as cf
 import os
@@ -58,6 +61,23 @@ def build(verbose=False, force=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     return LIB
+
+
+EXT_NAME = "inscy_gb300_ext"
+EXT_DIR = os.path.join(OBJ, "ext")
+
+
+def build_ext(verbose=False):
+    """Compile (or reuse) the PyTorch binding and return the loaded module.
+
+    The module only binds: run_gpu_4 / run_gpu_5 call the C ABI of
+    libinscy_gb300.so, which it links with an rpath to this directory."""
+    build()
+    from torch.utils import cpp_extension
+    os.makedirs(EXT_DIR, exist_ok=True)
+    return cpp_extension.load(name=EXT_NAME, sources=[os.path.join(CSRC, "torch_binding.cpp")],
+                              extra_cflags=["-O2"], extra_ldflags=["-L" + HERE, "-linscy_gb300", "-Wl,-rpath," + HERE],
+                              build_directory=EXT_DIR, with_cuda=True, verbose=verbose)
 
 
 if __name__ == "__main__":

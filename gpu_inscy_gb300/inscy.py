@@ -13,7 +13,7 @@ reference's behaviour (python/inscy.py:37-107).
 """
 import numpy as np
 
-from . import _lib
+from . import _ext, _lib
 
 
 def _as_numpy(X):
@@ -28,6 +28,16 @@ def _as_numpy(X):
 
 def _run(X, neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectangular, entropy_order, mode,
          as_numpy):
+    if not as_numpy:
+        # the reference-facing call: the PyTorch extension's run_gpu_4 /
+        # run_gpu_5, whose result is already the reference's pair of lists
+        import torch
+        Xt = X if isinstance(X, torch.Tensor) else torch.from_numpy(_as_numpy(X))
+        ext = _ext.load()
+        fn = ext.run_gpu_5 if mode == _lib.MODE_BATCHED else ext.run_gpu_4
+        subspaces, clusterings = fn(Xt, neighborhood_size, F, num_obj, min_size, r, number_of_cells,
+                                    bool(rectangular), entropy_order)
+        return subspaces, clusterings
     p = _lib.make_params(neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectangular, entropy_order)
     try:
         import torch
@@ -38,19 +48,20 @@ def _run(X, neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectang
             stream = torch.cuda.current_stream(Xc.device).cuda_stream
             with torch.cuda.device(Xc.device):
                 subs, labels, stats = _lib.run_device(Xc.data_ptr(), Xc.shape[0], Xc.shape[1], p, stream, mode)
-            return (subs, labels) if as_numpy else (subs, [l.tolist() for l in labels])
+            return subs, labels
     except ImportError:  # pragma: no cover
         pass
     subs, labels, stats = _lib.run_host(_as_numpy(X), p, mode)
-    return (subs, labels) if as_numpy else (subs, [l.tolist() for l in labels])
+    return subs, labels
 
 
 def GPU(X, neighborhood_size, F, num_obj, min_size, r=1., number_of_cells=3, rectangular=False, entropy_order=0,
         as_numpy=False):
     """Plain GPU INSCY (replaces python/inscy.py:189 GPU -> run_gpu_4).
 
-    Returns (subspaces, clusterings) as Python lists like the reference; with
-    as_numpy=True the clusterings are a list of int32 arrays (no copy)."""
+    Returns (subspaces, clusterings) as Python lists like the reference,
+    through the PyTorch extension's run_gpu_4; with as_numpy=True, through the
+    C ABI directly, the clusterings are a list of int32 arrays (no copy)."""
     return _run(X, neighborhood_size, F, num_obj, min_size, r, number_of_cells, rectangular, entropy_order,
                 _lib.MODE_PLAIN, as_numpy)
 

@@ -12,7 +12,8 @@ Only the host-side entry `run_cpu3_weak` (`inscy_map.cpp:230-270`) of the
 built module is ever called: it is the reference CPU INSCY that pins the
 oracle restatement through the golden fixtures in `tests/golden/`.
 
-Usage:  python oracle/build_ref.py [REFERENCE_ROOT]
+Usage:  python oracle/build_ref.py REFERENCE_ROOT
+        (or REFERENCE_ROOT in the environment variable INSCY_REFERENCE_ROOT)
 """
 import os
 import sys
@@ -48,8 +49,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 
 
-def load(ref_root="/root/reference", verbose=False):
+def reference_root(arg=None):
+    """The reference's source tree: the argument, else INSCY_REFERENCE_ROOT."""
+    root = arg or os.environ.get("INSCY_REFERENCE_ROOT")
+    if not root or not os.path.isdir(root):
+        raise RuntimeError("the reference's sources are needed: pass their root or set INSCY_REFERENCE_ROOT")
+    return root
+
+
+def load(ref_root=None, verbose=False):
     """Build (or reuse) the reference module and return it."""
+    ref_root = reference_root(ref_root)
     from torch.utils.cpp_extension import load as _load
     os.makedirs(OUT, exist_ok=True)
     os.environ.setdefault("TORCH_CUDA_ARCH_LIST", "10.0")
@@ -64,7 +74,7 @@ def load(ref_root="/root/reference", verbose=False):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
     t0 = time.time()
     load(root, verbose=True)
     print("reference module built in %.1f s -> %s" % (time.time() - t0, OUT))

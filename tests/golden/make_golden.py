@@ -4,8 +4,9 @@ Runs the reference's own `run_cpu3_weak` (`inscy_map.cpp:230-270`, the
 function behind `python/inscy.py:121 CPU()`) built by
 `oracle/build_ref.py`, on seeded inputs, and stores inputs, parameters and
 outputs as compressed .npz files next to this script.  Needs the reference
-sources (only present where the fixtures are made); the tests only read the
-.npz files.
+sources (only present where the fixtures are made; their root in the
+environment variable INSCY_REFERENCE_ROOT); the tests only read the .npz
+files.
 
 Fixtures:
   small_rect{0,1}.npz  the 1,500 x 5 workload (4 clusters in 3-dim subspaces,

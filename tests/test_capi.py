@@ -87,3 +87,18 @@ def test_missing_library_fails_loudly(monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(ImportError):
         _lib.load()
+
+
+def test_torch_binding_builds_with_the_reference_entry_points():
+    """The PyTorch extension (the Python binding of the engine) compiles
+    against the library and exports the reference extension's run_gpu_4 /
+    run_gpu_5 (inscy_map.cpp:979-1158) with its argument names."""
+    pytest.importorskip("torch")
+    from gpu_inscy_gb300 import _ext
+    ext = _ext.load()
+    assert ext.version() == _lib.load().inscy_version().decode()
+    for name in ("run_gpu_4", "run_gpu_5"):
+        doc = getattr(ext, name).__doc__
+        for arg in ("X", "neighborhood_size", "F", "num_obj", "min_size", "r", "number_of_cells", "rectangular",
+                    "entropy_order"):
+            assert arg + ":" in doc, (name, arg)

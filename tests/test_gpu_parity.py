@@ -130,6 +130,22 @@ def test_drop_in_api_returns_reference_types(engine):
     assert_same((subs5, clus5), want, "GPU5() with a device tensor")
 
 
+@pytest.mark.parametrize("rect", [0, 1])
+def test_torch_binding_matches_reference_outputs(engine, rect):
+    """The PyTorch extension's run_gpu_4 / run_gpu_5 (the reference-facing
+    binding) on host and device tensors give the reference's own outputs."""
+    torch = pytest.importorskip("torch")
+    from gpu_inscy_gb300 import _ext
+    ext = _ext.load()
+    X, p, want = small_case(rect)
+    args = (p["neighborhood_size"], p["F"], p["num_obj"], p["min_size"], p["r"], p["number_of_cells"],
+            p["rectangular"], p["entropy_order"])
+    assert_same(tuple(ext.run_gpu_4(torch.from_numpy(X), *args)), want, "run_gpu_4, host tensor")
+    assert_same(tuple(ext.run_gpu_5(torch.from_numpy(X).cuda(), *args)), want, "run_gpu_5, device tensor")
+    with pytest.raises(RuntimeError):
+        ext.run_gpu_5(torch.from_numpy(X).cuda(), *args[:-1], 1)  # entropy_order != 0 is refused
+
+
 def test_batch_entry(engine):
     cases = [_random_case(s) for s in (11, 12, 13)]
     p = cases[0][1]
