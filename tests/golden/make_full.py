@@ -14,6 +14,8 @@ Usage:  python tests/golden/make_full.py plain batch large_d   (any subset)
   batch    8 datasets of the 64-dataset batch workload, seed 0, including
            the largest (48,807 x 20)                  -> full_batch.json
   large_d  the 100,000 x 25 workload, seed 0           -> full_large_d.json
+  large_d_20k  the same generator and parameters at 20,000 points (d = 25,
+           cells = 5, eps = 0.02), seed 0             -> full_large_d_20k.json
 """
 import json
 import os
@@ -58,6 +60,12 @@ def main(which):
                       index=i) for i in BATCH_PICK]
         with open(os.path.join(HERE, "full_batch.json"), "w") as f:
             json.dump({"workload": "batch64_seed0", "entries": ents}, f)
+    if "large_d_20k" in which:
+        X = synth.make_large_d(0, n=20_000)
+        out = {"workload": "large_d_n20000_d25", "entries": [entry("large_d_20k_seed0", X, dict(synth.PARAMS["large_d"]),
+                                                                   generator="make_large_d", seed=0, n_arg=20_000)]}
+        with open(os.path.join(HERE, "full_large_d_20k.json"), "w") as f:
+            json.dump(out, f)
     if "large_d" in which:
         X = synth.make_large_d(0)
         out = {"workload": "large_d_n100000_d25", "entries": [entry("large_d_seed0", X, dict(synth.PARAMS["large_d"]),

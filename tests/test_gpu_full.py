@@ -23,6 +23,8 @@ pytestmark = pytest.mark.gpu
 def regenerate(e):
     if e["generator"] == "make_batch":
         X = synth.make_batch(e["seed"])[e["index"]]
+    elif "n_arg" in e:
+        X = getattr(synth, e["generator"])(e["seed"], n=e["n_arg"])
     else:
         X = getattr(synth, e["generator"])(e["seed"])
     assert X.shape == (e["n"], e["d"])
@@ -66,6 +68,17 @@ def test_batched_form_matches_oracle(engine):
                     reason="the 100,000 x 25 fixture was not made")
 def test_large_d_workload_matches_oracle(engine):
     e = full_fixture("large_d")["entries"][0]
+    X = regenerate(e)
+    subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]))
+    assert_digest(subs, labels, e, e["name"])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "full_large_d_20k.json")),
+                    reason="the 20,000 x 25 fixture was not made")
+def test_large_d_generator_at_20000_points_matches_oracle(engine):
+    """The 100,000 x 25 workload's generator and parameters (d = 25: 32-slot
+    point rows; cells = 5; eps = 0.02) at 20,000 points."""
+    e = full_fixture("large_d_20k")["entries"][0]
     X = regenerate(e)
     subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]))
     assert_digest(subs, labels, e, e["name"])
