@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -77,6 +78,16 @@ constexpr long long kSinglePassBytes = INSCY_SINGLE_PASS_BYTES;
 #define INSCY_DENSITY_ROWS 1
 #endif
 constexpr bool kDensityRows = INSCY_DENSITY_ROWS != 0;
+// Candidate rows of the row kernel: prefetched into registers through L1
+// (default), or gathered by TMA tile::gather4 copies into shared memory when
+// the environment variable INSCY_ROWS_TMA is 1 at the start of a run.  Both
+// write the same lists; the TMA form measured 3.6x slower on the 25,000 x 15
+// workload (its copies go from L2 to shared memory and lose the L1 reuse of
+// the candidate rows that neighbouring queries share).
+static bool rows_tma_requested() {
+  const char* e = std::getenv("INSCY_ROWS_TMA");
+  return e && e[0] == '1';
+}
 // narrowest leaf key the level kernel may use (4; raised only to test the wider forms)
 #ifndef INSCY_TREE_MIN_KEY_BYTES
 #define INSCY_TREE_MIN_KEY_BYTES 4
@@ -576,6 +587,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   }
   const int ni = (int)n;
   const int cells = hp.cells;
+  const bool rows_tma = rows_tma_requested();
   const int G = (int)std::ceil(1.0 / (double)hp.eps);  // inscy_map.cpp:243
   if (G > 256) throw Error(INSCY_ERR_LIMIT, "ceil(1/neighborhood_size) = " + std::to_string(G) + " > 256");
   const float csz = 1.0f / (float)cells;
@@ -948,6 +960,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.items = nullptr;
       DL.phi_work = dphiwork;
       DL.sms = sms_;
+      DL.rows_tma = rows_tma ? 1 : 0;
       auto neighbours = [&](bool write) {
         if (level == 1) {
           launch_neighbours(DL, write, s);

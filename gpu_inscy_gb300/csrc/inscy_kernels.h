@@ -73,6 +73,7 @@ struct DensityLaunch {
   RowItem* items;                   // row kernel: one record per (group, query), written by the capacity kernel
   unsigned long long* phi_work;     // scratch of the phi kernels (kPhiWorkBytes, zeroed by the caller before each launch)
   int sms;                          // SMs of the device: persistent grids fill each once
+  int rows_tma;                     // levels >= 2, d <= 32: gather the candidate rows with TMA (k_neighbours_rows_tma)
   long long prev_total;
   long long total;
   long long prev_nkeep;

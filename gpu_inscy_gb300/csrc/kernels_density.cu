@@ -25,6 +25,9 @@
 #include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
+#ifdef __CUDACC__
+#include <cuda.h>  // CUtensorMap (the type only: the encoder is reached through the runtime)
+#endif
 
 #include "inscy_common.cuh"
 #include "inscy_kernels.h"
@@ -514,6 +517,222 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
   }
 }
 
+#ifdef __CUDACC__
+// ---------------------------------------------------------------------------
+// The same pass with the candidate rows gathered by the tensor memory
+// accelerator.  Each warp owns kRB chunk buffers in shared memory; the rows of
+// chunk j (32 candidates, by id) arrive in buffer j % kRB through eight
+// cp.async.bulk.tensor tile::gather4 copies (four rows each, issued by lanes
+// 0..7), counted in by that buffer's mbarrier, while the warp tests chunk
+// j - kRB + 1 ... j - 1.  The candidates' ids and partial distances go to the
+// buffer's side arrays when the copies are issued.  Tests, writes and outputs
+// are those of k_neighbours_rows.
+// ---------------------------------------------------------------------------
+#ifndef INSCY_ROWS_TMA_BUFFERS16
+#define INSCY_ROWS_TMA_BUFFERS16 3
+#endif
+__host__ __device__ constexpr int rows_tma_buffers(int kS) { return kS == 16 ? INSCY_ROWS_TMA_BUFFERS16 : 2; }
+__host__ __device__ constexpr int rows_tma_blocks(int kS) { return 3; }
+__host__ __device__ constexpr int rows_tma_smem(int kS) { return 8 * rows_tma_buffers(kS) * 32 * kS * 4; }
+// an mbarrier wait gives up after this many polls (the copies of a chunk take
+// microseconds), reports guard code 36 and stops the warp
+constexpr int kMbarPolls = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity) {
+  for (int it = 0; it < kMbarPolls; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_addr(m)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <int kMode, int kS>
+__global__ void __launch_bounds__(256, rows_tma_blocks(kS))
+    k_neighbours_rows_tma(DensityArgs a, const __grid_constant__ CUtensorMap rows) {
+  constexpr bool kWrite = kMode >= 1;
+  constexpr int kQ = kS / 4;
+  constexpr int kRB = rows_tma_buffers(kS);
+  constexpr int kChunkFloats = 32 * kS;
+  constexpr uint32_t kChunkBytes = 32u * kS * 4u;
+  extern __shared__ __align__(128) unsigned char rows_smem[];
+  __shared__ __align__(8) uint64_t mbar[8][kRB];
+  __shared__ int sq[8][kRB][32];      // per warp and buffer: the candidates' ids
+  __shared__ float sacc[8][kRB][32];  // and their partial distances
+  __shared__ float4 squery[8][kS];
+  __shared__ unsigned long long sstat[8][3];
+  const unsigned lane = lane_id();
+  const unsigned lt = lanemask_lt();
+  const int wb = (int)(threadIdx.x >> 5);
+  constexpr bool single = kMode == 2;
+  float* wrows = reinterpret_cast<float*>(rows_smem) + (size_t)wb * kRB * kChunkFloats;
+  const float4* qv = squery[wb];
+  const float acc_max = a.acc_max;
+  const int sentinel = a.n;  // row n of the rows: coordinates 3.4e38, no test passes
+  if (lane == 0) {
+    sstat[wb][0] = sstat[wb][1] = sstat[wb][2] = 0;
+    for (int b = 0; b < kRB; ++b)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&mbar[wb][b])), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  uint32_t ph = 0;  // bit b: the parity the next wait on buffer b waits for
+  bool stuck = false;
+  for (;;) {
+    unsigned long long take = 0;
+    if (lane == 0) take = atomicAdd(a.work, (unsigned long long)a.chunk);
+    const long long w0 = (long long)__shfl_sync(0xffffffffu, take, 0);
+    if (w0 >= a.nwarps) break;
+    const long long w1 = w0 + a.chunk < a.nwarps ? w0 + a.chunk : a.nwarps;
+    for (long long w = w0; w < w1 && !stuck; ++w) {
+      const RowItem r = a.items[w];
+      if (r.len < 0) continue;  // failed its checks (reported by the capacity kernel)
+      const int p = r.p, nc = r.nc, D0 = r.d0;
+      const long long len = r.len;
+      const int2* ents = a.prev_ent + r.pb;
+      const long long item_c = (int)lane < nc ? a.subs[r.sub_base + lane].item_off + r.i : 0;
+      int run = 0;
+      long long ob = 0;
+      if (single) {
+        const long long cb = a.cap_base[w];
+        if (!GUARD_OK(a.guard, cb >= 0 && cb + (long long)nc * len <= a.total, 39, cb)) continue;
+        ob = cb + (long long)lane * len;
+      } else if (kWrite) {
+        if ((int)lane < nc) ob = a.loff[item_c];
+      }
+      __syncwarp();  // the previous pair's reads of the query slot are done
+      if (lane < (unsigned)kS) {
+        const size_t t = (size_t)p * kS + lane;
+        squery[wb][lane] = make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
+      }
+      const long long nchunks = (len + 31) >> 5;
+      // entry of chunk j for this lane (lanes past the end: the sentinel)
+      auto entry = [&](long long j) -> int2 {
+        const long long k = (j << 5) + lane;
+        return k < len ? ents[k] : make_int2(sentinel, 0);
+      };
+      int2 e_next = nchunks > 0 ? entry(0) : make_int2(sentinel, 0);
+      // chunk j into buffer j % kRB: ids and distances to the side arrays,
+      // then the rows by eight 4-row gathers
+      auto issue = [&](long long j) {
+        const int b = (int)(j % kRB);
+        int q = e_next.x;
+        if (q != sentinel && !GUARD_OK(a.guard, q >= 0 && q < a.n, 34, q)) q = sentinel;
+        sq[wb][b][lane] = q;
+        sacc[wb][b][lane] = __int_as_float(e_next.y);
+        if (j + 1 < nchunks) e_next = entry(j + 1);
+        const int g = (int)(lane & 7u) * 4;
+        const int r0 = __shfl_sync(0xffffffffu, q, g), r1 = __shfl_sync(0xffffffffu, q, g + 1);
+        const int r2 = __shfl_sync(0xffffffffu, q, g + 2), r3 = __shfl_sync(0xffffffffu, q, g + 3);
+        uint64_t* mb = &mbar[wb][b];
+        // the warp's reads of buffer b (generic proxy) before the copies
+        // (async proxy) overwrite it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mb)), "r"(kChunkBytes)
+                       : "memory");
+        __syncwarp();
+        if (lane < 8u) {
+          float* dst = wrows + (size_t)b * kChunkFloats + (size_t)lane * 4 * kS;
+          asm volatile(
+              "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
+              " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(dst)),
+              "l"(reinterpret_cast<uint64_t>(&rows)), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_addr(mb))
+              : "memory");
+        }
+      };
+      for (long long j = 0; j < nchunks && j < kRB; ++j) issue(j);
+      __syncwarp();  // the query slot is visible to the whole warp
+      long long k = 0;
+      for (; k < nchunks; ++k) {
+        const int b = (int)(k % kRB);
+        // every lane polls; the warp goes on only if all of them saw the
+        // copies land (the decision stays warp-uniform)
+        if (!__all_sync(0xffffffffu, mbar_wait(&mbar[wb][b], (ph >> b) & 1u))) {
+          if (lane == 0) GUARD_OK(a.guard, false, 36, k);
+          stuck = true;
+          break;
+        }
+        ph ^= 1u << b;
+        const int q = sq[wb][b][lane];
+        const float acc = sacc[wb][b][lane];
+        const float4* xr = reinterpret_cast<const float4*>(wrows + (size_t)b * kChunkFloats + (size_t)lane * kS);
+        float xq[kS];
+#pragma unroll
+        for (int t = 0; t < kQ; ++t) {
+          if (4 * t + 3 >= D0) {
+            const float4 x = xr[t];
+            xq[4 * t] = x.x;
+            xq[4 * t + 1] = x.y;
+            xq[4 * t + 2] = x.z;
+            xq[4 * t + 3] = x.w;
+          } else {
+            xq[4 * t] = xq[4 * t + 1] = xq[4 * t + 2] = xq[4 * t + 3] = 0.f;
+          }
+        }
+#pragma unroll
+        for (int D = 0; D < kS; ++D) {
+          const int c = D - D0;
+          if (c < 0 || c >= nc) continue;  // warp-uniform
+          const float4 v = qv[D];
+          const float xd = xq[D];
+          const float acc2 = dist_step(acc, v.x, xd);
+          const bool ok = xd >= v.y && xd < v.z && acc2 <= acc_max;
+          const unsigned m = __ballot_sync(0xffffffffu, ok);
+          if (!m) continue;
+          if (kWrite) {
+            const long long base = __shfl_sync(0xffffffffu, ob + run, c);
+            if (ok) {
+              const long long o = base + __popc(m & lt);
+              if (single || GUARD_OK(a.guard, o >= 0 && o < a.total, 35, o))
+                a.ent[o] = make_int2(q, __float_as_int(acc2));
+            }
+          }
+          if ((int)lane == c) run += __popc(m);
+        }
+        __syncwarp();  // every lane has read buffer b
+        if (k + kRB < nchunks) issue(k + kRB);
+      }
+      if (stuck) {
+        // the copies still in flight land before the warp leaves
+        for (long long j = k; j < nchunks && j < k + kRB; ++j) {
+          const int b = (int)(j % kRB);
+          if (mbar_wait(&mbar[wb][b], (ph >> b) & 1u)) ph ^= 1u << b;
+        }
+        break;
+      }
+      if (!kWrite || single) {
+        int out = 0;
+        if ((int)lane < nc) {
+          a.cnt[item_c] = run;
+          if (single) a.cap_loff[item_c] = ob;
+          out = run;
+        }
+        for (int o = 16; o > 0; o >>= 1) out += __shfl_xor_sync(0xffffffffu, out, o);
+        if (lane == 0) {
+          sstat[wb][0] += (unsigned long long)len * nc;
+          sstat[wb][1] += (unsigned long long)len;
+          sstat[wb][2] += (unsigned long long)out;
+        }
+      }
+    }
+    if (stuck) break;
+  }
+  if ((!kWrite || single) && lane == 0) {
+    if (a.cand_counter) atomicAdd(a.cand_counter, sstat[wb][0]);
+    if (a.list_counter) atomicAdd(a.list_counter, sstat[wb][1]);
+    if (single && a.out_counter) atomicAdd(a.out_counter, sstat[wb][2]);
+  }
+}
+#endif  // __CUDACC__
+
+
 // single-pass list capacity of every (group, query): children x the query's
 // parent-list length; with `a.items`, also the pair's record for the row
 // kernel (query point, parent list, children), checked here once
@@ -990,11 +1209,80 @@ void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned
   k_phi_selftest<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, seed, bad);
 }
 
+#ifdef __CUDACC__
+// The row table as a 2-d tensor of n + 1 rows of `slots` floats (the last
+// row is the sentinel), read one row per box by tile::gather4 copies.
+static bool rows_tensor_map(CUtensorMap* tm, const float* xrow, int n, int slots) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                              const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    encode = reinterpret_cast<Encode>(fn);
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)slots, (cuuint64_t)n + 1};
+  const cuuint64_t strides[1] = {(cuuint64_t)slots * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)slots, 1};  // one row per box, as tile::gather4 takes it
+  const cuuint32_t estr[2] = {1, 1};
+  return encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(xrow), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int kMode, int kS>
+static void rows_tma_kernel(const DensityArgs& a, const CUtensorMap& tm, unsigned blocks, cudaStream_t s) {
+  static bool attr = false;  // the dynamic shared memory above 48 KB is opted into once
+  if (!attr) {
+    cudaFuncSetAttribute(k_neighbours_rows_tma<kMode, kS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         rows_tma_smem(kS));
+    attr = true;
+  }
+  k_neighbours_rows_tma<kMode, kS><<<blocks, 256, rows_tma_smem(kS), s>>>(a, tm);
+}
+
+// The row kernel with TMA-gathered rows; false when the tensor map cannot be
+// made (the caller then launches k_neighbours_rows).
+static bool rows_tma_launch(const DensityLaunch& L, DensityArgs& a, long long nwarps, bool write, cudaStream_t s) {
+  CUtensorMap tm;
+  if (!rows_tensor_map(&tm, L.xrow, L.n, L.slots)) return false;
+  const long long max_blocks = (long long)(L.sms > 0 ? L.sms : 1) * rows_tma_blocks(L.slots);
+  long long chunk = nwarps / (max_blocks * 8 * 16);
+  a.chunk = (int)(chunk < 1 ? 1 : chunk > 8 ? 8 : chunk);
+  const long long need = (nwarps + 7) / 8;
+  const unsigned blocks = (unsigned)(need < max_blocks ? need : max_blocks);
+  const int mode = write ? (L.cap_base ? 2 : 1) : 0;
+  if (L.slots == 16) {
+    if (mode == 2) rows_tma_kernel<2, 16>(a, tm, blocks, s);
+    else if (mode == 1) rows_tma_kernel<1, 16>(a, tm, blocks, s);
+    else rows_tma_kernel<0, 16>(a, tm, blocks, s);
+  } else if (L.slots == 24) {
+    if (mode == 2) rows_tma_kernel<2, 24>(a, tm, blocks, s);
+    else if (mode == 1) rows_tma_kernel<1, 24>(a, tm, blocks, s);
+    else rows_tma_kernel<0, 24>(a, tm, blocks, s);
+  } else {
+    if (mode == 2) rows_tma_kernel<2, 32>(a, tm, blocks, s);
+    else if (mode == 1) rows_tma_kernel<1, 32>(a, tm, blocks, s);
+    else rows_tma_kernel<0, 32>(a, tm, blocks, s);
+  }
+  return true;
+}
+#endif
+
 // level >= 2: one warp per (parent group, query point)
 void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s) {
   if (nwarps <= 0) return;
   DensityArgs a = make_args(L);
   a.nwarps = nwarps;
+#ifdef __CUDACC__
+  if (L.rows_tma && L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 24 || L.slots == 32) &&
+      L.d <= L.slots && rows_tma_launch(L, a, nwarps, write, s))
+    return;
+#endif
   if (L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 24 || L.slots == 32) && L.d <= L.slots) {
     // persistent warps: a grid that fills every SM once, (group, query) pairs
     // handed out by the work counter, several per update when there are many

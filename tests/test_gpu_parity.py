@@ -146,6 +146,21 @@ def test_torch_binding_matches_reference_outputs(engine, rect):
         ext.run_gpu_5(torch.from_numpy(X).cuda(), *args[:-1], 1)  # entropy_order != 0 is refused
 
 
+def test_tma_row_gather_writes_the_same_lists(engine, monkeypatch):
+    """The row kernel with its candidate rows gathered by TMA (tile::gather4
+    into shared memory, INSCY_ROWS_TMA=1) gives the reference's outputs: the
+    16-slot rows of the small workload and the 24- and 32-slot rows of the
+    wide fixtures."""
+    monkeypatch.setenv("INSCY_ROWS_TMA", "1")
+    for rect in (0, 1):
+        X, p, want = small_case(rect)
+        got, _ = gpu_run(X, **p)
+        assert_same(got, want, "TMA rows, small rect=%d" % rect)
+    for i, X, p, want in wide_cases()[:4]:
+        got, _ = gpu_run(X, **p)
+        assert_same(got, want, "TMA rows, wide %d (d=%d)" % (i, X.shape[1]))
+
+
 def test_batch_entry(engine):
     cases = [_random_case(s) for s in (11, 12, 13)]
     p = cases[0][1]
