@@ -1684,6 +1684,7 @@ bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
       const int* esz = E.size.data();
       int j = 0;
       for (; j < m; ++j) {
+        if (j + 16 < m) __builtin_prefetch(lab + pts[j + 16]);  // random reads of an n-long vector
         const int l = lab[pts[j]];
         if (l >= 0) {
           const int v = esz[l];
@@ -1741,7 +1742,19 @@ void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState
   // before the writes.
   const int first = st.nlabels + 1;
   long long work = 0;
+  // three dependent random reads per component (its member range, its first
+  // member, that member's label): each is prefetched a few components ahead
+  // of its use, the next read in the chain once the previous one has landed
+  const int* mem = hs.members.data();
+  const long long* moff = hs.moff.data();
+  const uint64_t* lv = V.gv.data();
   for (int t = 0; t < c.norder; ++t) {
+    if (t + 16 < c.norder) __builtin_prefetch(moff + order[t + 16]);
+    if (t + 8 < c.norder) __builtin_prefetch(mem + moff[order[t + 8]]);
+    if (t + 4 < c.norder) {
+      const long long a4 = moff[order[t + 4]];
+      if (a4 < moff[order[t + 4] + 1]) __builtin_prefetch(lv + mem[a4]);
+    }
     int comp = order[t];
     long long m0 = hs.moff[comp], m1 = hs.moff[comp + 1];
     if (m1 == m0) continue;
