@@ -553,6 +553,7 @@ class Engine {
   std::map<uint64_t, int> eidx_;              // subspace -> entry
   std::vector<std::vector<uint64_t>> dim_bits_;  // per dim: bitset of the entries whose subspace holds it
   std::vector<int> sup_;                         // superset_candidates' result
+  std::vector<int> prune_order_;                 // pruneRedundancy: superset entries by largest cluster
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<LoopVec> vbuf_;                  // one clustering vector per recursion depth
   std::vector<char> alive_;                    // join: clusters of the loop still alive
@@ -1674,8 +1675,18 @@ bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
   bool bits_set = false;  // the region's bitmap, built when first needed
   int max_min = 0;
   bool result = true;
-  for (int i : superset_candidates(smask)) {
+  // An entry's minimum (its smallest cluster touching the region) is at most
+  // its largest cluster, so once max_min reaches an entry's largest cluster
+  // the entry cannot raise it; visiting the entries by largest cluster,
+  // largest first, the scan stops at the first such entry.  The answer
+  // depends only on the maximum over the entries, not on their order.
+  std::vector<int>& order = prune_order_;
+  const std::vector<int>& sup = superset_candidates(smask);
+  order.assign(sup.begin(), sup.end());
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return ents_[x]->maxsz > ents_[y]->maxsz; });
+  for (int i : order) {
     Entry& E = *ents_[i];
+    if (E.maxsz <= max_min) break;
     int mn = -1;
     if (!use_bits) {
       // the entry matters only if its minimum ends above max_min, so the scan
