@@ -450,8 +450,33 @@ constexpr long long kParallelWalk = 32768;
 
 struct HostParams {
   float eps, F, r;
-  int num_obj, min_size, cells, rect;
+  int num_obj, min_size, cells, rect, entropy_order;
 };
+
+// get_subspace_order (inscy_map.cpp:61-121): the SCY-tree's level order.
+// Identity for entropy_order 0; else dims by ascending entropy of their
+// coarse-cell histogram (float sums of -p log p with p = count / n, float
+// log), ties by dim, reversed for entropy_order -1.  An empty cell makes
+// p log p a NaN exactly as in the reference; the (entropy, dim) pairs are
+// ordered by the same std::sort the reference's pairsort calls.
+std::vector<int> level_order_of(const std::vector<int>& hist, int n, int d, int cells, int entropy_order) {
+  std::vector<int> order(d);
+  for (int k = 0; k < d; ++k) order[k] = k;
+  if (entropy_order == 0) return order;
+  std::vector<std::pair<float, int>> e(d);
+  for (int k = 0; k < d; ++k) {
+    float h = 0.f;
+    for (int c = 0; c < cells; ++c) {
+      const float p = (float)hist[(size_t)k * cells + c] / (float)n;
+      h -= p * std::log(p);
+    }
+    e[k] = {h, k};
+  }
+  std::sort(e.begin(), e.end());
+  if (entropy_order == -1) std::reverse(e.begin(), e.end());
+  for (int k = 0; k < d; ++k) order[k] = e[k].second;
+  return order;
+}
 
 // host-pool workers of engines created on this thread (-1: by the core count)
 // and the single-pass list budget of their runs: batch lanes divide both
@@ -677,6 +702,22 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   };
   launch_prep(dX, ni, d, cells, csz, G, fsz, hp.eps, dcc, dfc, dgz, s);
   ++launches;
+  // the SCY-tree's and the neighbourhood trie's level order
+  std::vector<int> lvl_dim(d), lvl_pos(d);
+  {
+    std::vector<int> hist;
+    if (hp.entropy_order != 0) {
+      Scope tmp(*pool_, s);
+      int* dh = tmp.get<int>((size_t)d * cells);
+      CK(cudaMemsetAsync(dh, 0, sizeof(int) * (size_t)d * cells, s));
+      launch_cell_hist(dcc, ni, d, cells, sms_, dh, s);
+      ++launches;
+      hist.resize((size_t)d * cells);
+      d2h(hist.data(), dh, sizeof(int) * hist.size(), s);
+    }
+    lvl_dim = level_order_of(hist, ni, d, cells, hp.entropy_order);
+    for (int t = 0; t < d; ++t) lvl_pos[lvl_dim[t]] = t;
+  }
   // point rows for the density pass when a row fits 16, 24 or 32 slots
   float* dxrow = nullptr;
   float* dwin = nullptr;
@@ -736,11 +777,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     int* a = tmp.get<int>(n);
     int* b = tmp.get<int>(n);
     // neighbourhood-trie leaf order: lexicographic fine cells, dims in
-    // level order, ties by id -> LSD passes from the last dim
+    // level order, ties by id -> LSD passes from the last level
     launch_iota(a, ni, s);
     ++launches;
-    for (int k = d - 1; k >= 0; --k) {
-      launch_byte_sort_pass(a, b, ni, dfc, d, k, hist, htot, nullptr, sums, s);
+    for (int t = d - 1; t >= 0; --t) {
+      launch_byte_sort_pass(a, b, ni, dfc, d, lvl_dim[t], hist, htot, nullptr, sums, s);
       launches += 5;
       std::swap(a, b);
     }
@@ -768,11 +809,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     dcand = persist.get<int>((size_t)tot);
     launch_candidate_lists(ni, d, G, dbucket, dboff, drank, dfc, dcoff, dcand, s);
     ++launches;
-    // root SCY-tree leaf order: coarse cells in dim order, ties by id
+    // root SCY-tree leaf order: coarse cells in level order, ties by id
     launch_iota(a, ni, s);
     ++launches;
-    for (int k = d - 1; k >= 0; --k) {
-      launch_byte_sort_pass(a, b, ni, dcc, d, k, hist, htot, nullptr, sums, s);
+    for (int t = d - 1; t >= 0; --t) {
+      launch_byte_sort_pass(a, b, ni, dcc, d, lvl_dim[t], hist, htot, nullptr, sums, s);
       launches += 5;
       std::swap(a, b);
     }
@@ -846,6 +887,18 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
 
       // ---- 1. subspaces of this level: children of the calls' subspaces
       std::vector<SubDesc> subs;
+      // the neighbourhood trie's walk (ScyTreeNode.cu:896-934) tests dim D of
+      // parent dims pm + D only when pm, ascending, lies in level order and
+      // D's level follows the last of them
+      auto win_of = [&](uint64_t pm, int D) {
+        int last = -1;
+        for (uint64_t m = pm; m; m &= m - 1) {
+          const int e = __builtin_ctzll(m);
+          if (lvl_pos[e] <= last) return 0;
+          last = lvl_pos[e];
+        }
+        return lvl_pos[D] > last ? 1 : 0;
+      };
       std::map<int, int> child_base;  // parent subspace -> first child
       for (auto& c : F.hcalls) {
         auto it = child_base.find(c.sub);
@@ -867,6 +920,8 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
             S.query_off = qo;
             S.plist_base = 0;
             S.bitmap_off = 0;
+            S.win = win_of(pm, D);
+            S.pad = 0;
             subs.push_back(S);
           }
           c.child_sub = base;
@@ -899,7 +954,9 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
           g.sub_base = i;
           g.nchild = j - i;
           g.nquery = subs[i].nquery;
-          g.pad = 0;
+          g.nowin = 0;
+          for (int c = i; c < j && c - i < 32; ++c)
+            if (!subs[c].win) g.nowin |= (int)(1u << (c - i));
           wo += (long long)g.nchild * g.nquery;
           ngroup_warps += g.nquery;
           groups.push_back(g);
@@ -1191,6 +1248,13 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         TL.nbig = ditems ? (int)items_big.size() : 0;
         TL.items_small = ditems ? ditems + items_big.size() : nullptr;
         TL.nsmall = ditems ? (int)items_small.size() : 0;
+        for (int k = 0; k < kMaxDims; ++k) {
+          TL.lvl_pos[k] = (uint8_t)(k < d ? lvl_pos[k] : 0);
+          TL.lvl_dim[k] = (uint8_t)(k < d ? lvl_dim[k] : 0);
+          unsigned long long gt = 0;
+          for (int e = k + 1; e < d; ++e) gt |= 1ull << lvl_pos[e];
+          TL.gt_pos[k] = k < d ? gt : 0ull;
+        }
         stats_.ms_tree += timed(s, [&] { launch_tree_level(TL, s); });
         launches += (TL.nbig > 0 && TL.nsmall > 0) ? 2 : 1;
         int err = scalar(derr, s);
@@ -2060,8 +2124,6 @@ int check_params(int64_t n, int d, const inscy_params* p) {
   if (!(p->neighborhood_size > 0.f)) return fail(INSCY_ERR_ARG, "neighborhood_size must be > 0");
   if (p->number_of_cells <= 0) return fail(INSCY_ERR_ARG, "number_of_cells must be > 0");
   if (p->number_of_cells > 255) return fail(INSCY_ERR_LIMIT, "number_of_cells > 255");
-  if (p->entropy_order != 0)
-    return fail(INSCY_ERR_UNSUPPORTED, "entropy_order != 0 is not implemented on the GPU path");
   return INSCY_OK;
 }
 
@@ -2091,6 +2153,7 @@ int run_common(const float* X, bool on_device, int64_t n, int d, const inscy_par
     hp.min_size = p->min_size;
     hp.cells = p->number_of_cells;
     hp.rect = p->rectangular ? 1 : 0;
+    hp.entropy_order = p->entropy_order;
     std::unique_ptr<inscy_result> res(new inscy_result());
     res->n = n;
     g_engine->run(X, on_device, n, d, hp, (cudaStream_t)stream, res->dims, res->labels, res->stats);

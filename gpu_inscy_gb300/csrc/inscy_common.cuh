@@ -64,6 +64,13 @@ struct SubDesc {
   long long query_off;  // parent's kept-point list offset (level 1: unused)
   long long plist_base; // parent's list base (entry offsets are absolute)
   long long bitmap_off; // word offset of this subspace's flag bitmaps
+  // 1: candidates must lie within +-1 fine cell of the query on `dim`.  The
+  // neighbourhood trie's walk (ScyTreeNode.cu:896-934) tests a subspace dim
+  // only while the subspace's dims, in ascending order, appear in the trie's
+  // level order; under a permuted level order the dims after the first
+  // inversion are left to the distance test alone.
+  int win;
+  int pad;
 };
 
 // The children of one parent subspace (contiguous subspace indices).
@@ -73,7 +80,7 @@ struct GroupDesc {
   int sub_base;
   int nchild;
   int nquery;
-  int pad;
+  int nowin;  // bit c: child c takes no fine-cell test (its SubDesc::win is 0; children < 32)
 };
 
 // One (group, query) pair of a level >= 2 density pass, resolved once by the
@@ -88,7 +95,7 @@ struct alignas(16) RowItem {
   int i;         // query index within the group
   short d0;      // first child's dim
   short nc;      // children
-  int pad;
+  int nowin;     // the group's GroupDesc::nowin
 };
 
 // Device-side consistency checks: the first failed check records its code and

@@ -16,6 +16,8 @@ void launch_exclusive_scan_i2ll(const int* in, long long* out, long long n, long
 void launch_prep(const float* X, int n, int d, int cells, float csz, int G, float fsz, float eps, uint8_t* cc,
                  uint8_t* fc, unsigned long long* gz, cudaStream_t s);
 void launch_iota(int* a, int n, cudaStream_t s);
+// hist[k * cells + c] += points whose coarse cell on dim k is c (hist zeroed by the caller)
+void launch_cell_hist(const uint8_t* cc, int n, int d, int cells, int sms, int* hist, cudaStream_t s);
 // rows of `slots` (16, 24 or 32 >= d) coordinates and fine-cell windows per point
 void launch_point_rows(const float* X, const uint8_t* fc, int n, int d, int slots, int G, const float* fine_lo,
                        float* xrow, float* win, cudaStream_t s);
@@ -137,6 +139,12 @@ struct TreeLaunch {
   const int* items_small;
   int nsmall;
   int key_bytes;  // leaf key width: 4, 8 or 16 bytes (d * kbits bits must fit)
+  // the SCY-tree's level order (get_subspace_order, inscy_map.cpp:61-121):
+  // level of every dim, dim of every level, and per dim e the levels of the
+  // dims > e (restrict_node's inclusion test, ScyTreeNode.cu:285)
+  uint8_t lvl_pos[kMaxDims];
+  uint8_t lvl_dim[kMaxDims];
+  unsigned long long gt_pos[kMaxDims];
 };
 #ifndef INSCY_TREE_BIG
 #define INSCY_TREE_BIG 4096

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256) k_neighbours(DensityArgs a) {
     int q = ok ? (level1 ? ids[j] : e.x) : -1;
     if (ok && !GUARD_OK(a.guard, q >= 0 && q < a.n, 24, q)) ok = false;
     ok = ok && q != p;
-    if (ok && !level1) {
+    if (ok && !level1 && S.win) {
       int fq = a.fc[(size_t)q * a.d + D];
       ok = fq >= fp - 1 && fq <= fp + 1;
     }
@@ -282,10 +282,11 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
     const float* xrow_q = a.X + (size_t)q * a.d;
     const uint8_t* frow_q = a.fc + (size_t)q * a.d;
     for (int c = 0; c < nc; ++c) {
-      const int D = a.subs[g.sub_base + c].dim;
+      const SubDesc& Sc = a.subs[g.sub_base + c];
+      const int D = Sc.dim;
       const int fp = frow_p[D];
       const int fq = frow_q[D];
-      bool ok = in && q != p && fq >= fp - 1 && fq <= fp + 1;
+      bool ok = in && q != p && (!Sc.win || (fq >= fp - 1 && fq <= fp + 1));
       float acc2 = 0.f;
       if (ok) {
         acc2 = dist_step(acc, xrow_p[D], xrow_q[D]);
@@ -414,7 +415,11 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
       __syncwarp();  // the previous pair's reads of the query slot are done
       if (lane < (unsigned)kS) {
         const size_t t = (size_t)p * kS + lane;
-        squery[wb][lane] = make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
+        // a child without the fine-cell test gets the window (-inf, +inf)
+        const int c = (int)lane - D0;
+        const bool open = c >= 0 && c < nc && ((r.nowin >> c) & 1);
+        squery[wb][lane] = open ? make_float4(a.xrow[t], __uint_as_float(0xff800000u), __uint_as_float(0x7f800000u), 0.f)
+                                : make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
       }
       // candidate j of the list, one 8-byte entry (lanes past the end stand
       // on the sentinel row); nothing reads the loaded values until load_row,
@@ -609,7 +614,11 @@ __global__ void __launch_bounds__(256, rows_tma_blocks(kS))
       __syncwarp();  // the previous pair's reads of the query slot are done
       if (lane < (unsigned)kS) {
         const size_t t = (size_t)p * kS + lane;
-        squery[wb][lane] = make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
+        // a child without the fine-cell test gets the window (-inf, +inf)
+        const int c = (int)lane - D0;
+        const bool open = c >= 0 && c < nc && ((r.nowin >> c) & 1);
+        squery[wb][lane] = open ? make_float4(a.xrow[t], __uint_as_float(0xff800000u), __uint_as_float(0x7f800000u), 0.f)
+                                : make_float4(a.xrow[t], a.win[2 * t], a.win[2 * t + 1], 0.f);
       }
       const long long nchunks = (len + 31) >> 5;
       // entry of chunk j for this lane (lanes past the end: the sentinel)
@@ -763,7 +772,7 @@ __global__ void k_list_capacity(DensityArgs a, long long* __restrict__ cap) {
   r.i = (int)i;
   r.d0 = (short)a.subs[g.sub_base].dim;
   r.nc = (short)g.nchild;
-  r.pad = 0;
+  r.nowin = g.nowin;
   if (ok) {
     const int p = a.prev_keep[k];
     const long long pb = a.prev_loff[k];

@@ -162,6 +162,38 @@ void launch_iota(int* a, int n, cudaStream_t s) {
   if (n > 0) k_iota<<<(n + 255) / 256, 256, 0, s>>>(a, n);
 }
 
+// Points per (dim, coarse cell): the counts behind the entropy level order of
+// get_subspace_order (inscy_map.cpp:61-121), whose cell rule is the coarse
+// cell's.  Counts go to shared memory first when d * cells fit kHistShared.
+constexpr int kHistShared = 8192;
+__global__ void k_cell_hist(const uint8_t* __restrict__ cc, int n, int d, int cells, int* __restrict__ hist) {
+  __shared__ int sh[kHistShared];
+  const int m = d * cells;
+  const bool local = m <= kHistShared;
+  if (local)
+    for (int i = threadIdx.x; i < m; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const long long total = (long long)n * d;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(t % d);
+    const int c = cc[t];
+    if (c < cells) atomicAdd(local ? &sh[k * cells + c] : &hist[k * cells + c], 1);
+  }
+  __syncthreads();
+  if (local)
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+void launch_cell_hist(const uint8_t* cc, int n, int d, int cells, int sms, int* hist, cudaStream_t s) {
+  const long long total = (long long)n * d;
+  if (total <= 0) return;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 4LL * sms) blocks = 4LL * sms;
+  k_cell_hist<<<(unsigned)blocks, 256, 0, s>>>(cc, n, d, cells, hist);
+}
+
 void launch_scatter_rank(const int* order, int n, int* rank, cudaStream_t s) {
   if (n > 0) k_scatter_rank<<<(n + 255) / 256, 256, 0, s>>>(order, n, rank);
 }

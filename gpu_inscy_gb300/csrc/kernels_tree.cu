@@ -3,29 +3,40 @@
 // A call's SCY-tree (ScyTreeNode.h:25-121) is held as
 //   * its points, stored in the tree's leaf order (get_points,
 //     ScyTreeNode.cu:853-869): lexicographic in the cells of the remaining
-//     dims, then the cells of the restricted dims from the last restricted
-//     one back to the first, then point id;
+//     dims taken in the tree's level order (get_subspace_order,
+//     inscy_map.cpp:61-121; the identity unless entropy_order != 0), then the
+//     cells of the restricted dims from the last restricted one back to the
+//     first, then point id;
 //   * its "detached ghosts": s-connection chains (ScyTreeNode.cu:34-49)
-//     whose point was pruned earlier but whose chain is still in the trie.
+//     whose point was pruned earlier but whose chain is still in the trie,
+//     each as (point, marker dim g | last level << 8).
 //     The chains of points still present are implied by the per-point ghost
-//     flags.
+//     flags; where they end follows from the call's restricted dims alone.
+// A chain holds the trie levels from its marker's down to its last one.
+// restrict_node (ScyTreeNode.cu:227-323) keeps a node whose level's dim is
+// larger than the restricted dim D even when no point below it lies in the
+// restricted cell (`is_included`, :285), and a node above such a node.  In
+// the identity level order no such node lies above D's level and chains stay
+// whole; in a permuted order restrict leaves count-0 "phantom" nodes above
+// D's level and cuts chains to the levels that still hold a kept node.
 // Given that representation, the reference's pointer-trie operations become:
-//   restrict(D, c)            keep points with cell c on D
-//                             (ScyTreeNode.cu:227-379); a ghost whose chain
-//                             starts on D and lies in cell c marks the result
-//                             s-connected, other ghosts survive when their
-//                             point's cell on D is c;
+//   restrict(D, c)            keep points with cell c on D; a chain whose
+//                             marker is on D and lies in cell c marks the
+//                             result s-connected; other chains are cut
+//                             (chain_cut) and may survive as phantoms;
 //   mergeWithNeighbors        absorb cell c+1 while the tree restricted last was
 //                             s-connected (ScyTreeNode.cu:837-851); the merged
 //                             leaf order is a stable sort by (remaining cells,
-//                             cell on D); when no dim remains and the first
-//                             cell is empty the absorbed points are lost, as
-//                             mergeNodes adds points only to a node whose
-//                             count is positive (ScyTreeNode.cu:805-808);
+//                             cell on D); mergeNodes adds points only to a node
+//                             whose count is positive (ScyTreeNode.cu:805-808),
+//                             so the absorbed points of a leaf node that the
+//                             first cell left empty (a phantom, or the root when
+//                             no dim remains) are lost;
 //   pruneRecursionAndRemove2  keep weak-dense points (ScyTreeNode.cu:582-667);
 //                             propergate_count2 (:446-467) then erases empty
-//                             child nodes together with the s-connection of the
-//                             same cell, which decides which ghosts survive.
+//                             child nodes (phantoms included) together with the
+//                             s-connection of the same cell, which decides which
+//                             ghosts survive.
 // All of this is integer work: filters are block-wide stable compactions and
 // the merge re-sort is a stable counting-sort per dim (warp match + block
 // scan).
@@ -77,7 +88,46 @@ struct TreeArgs {
   long long pts_in_total;
   long long ghosts_in_total;
   Guard guard;
+  uint8_t lvl_pos[kMaxDims];             // trie level of every dim
+  uint8_t lvl_dim[kMaxDims];             // dim of every trie level
+  unsigned long long gt_pos[kMaxDims];   // per dim e: the levels whose dim is > e
 };
+
+// trie levels a .. b as a bit mask (empty when a > b)
+__device__ __forceinline__ unsigned long long level_span(int a, int b) {
+  if (a > b) return 0ull;
+  const unsigned long long hi = b >= 63 ? ~0ull : ((1ull << (b + 1)) - 1ull);
+  return hi & ~((1ull << a) - 1ull);
+}
+__device__ __forceinline__ int top_level(unsigned long long x) { return 63 - __clzll((long long)x); }
+
+// A chain from marker level pg to last level pt after restrict(D) removed
+// level pD (rem: the levels left; gt: the levels whose dim is > D; match: its
+// point's cell on D is among the restricted ones).  restrict_node keeps a
+// chain node whose dim is > D or that has a kept node below; at level pD it
+// keeps the node of a restricted cell, whose ancestors are then kept too, and
+// reaches nothing below another cell (ScyTreeNode.cu:227-323).  Returns the
+// new last level, or -1 when the chain is gone (a chain whose marker is on D
+// marks the tree s-connected and is not kept).
+__device__ __forceinline__ int chain_cut(int pg, int pt, int pD, unsigned long long rem, unsigned long long gt,
+                                         bool match) {
+  if (pD == pg) return -1;
+  unsigned long long x;
+  if (pD < pg) {  // below D's level, under the node of its point's cell on D
+    if (!match) return -1;
+    x = rem & gt & level_span(pg, pt);
+  } else if (pD <= pt) {  // passes D's level
+    if (match) {
+      x = rem & gt & level_span(pD + 1, pt);
+      if (!x) x = rem & level_span(pg, pD - 1);  // holds pg
+    } else {
+      x = rem & gt & level_span(pg, pD - 1);
+    }
+  } else {  // ends above D's level: kept in every restricted cell
+    x = rem & gt & level_span(pg, pt);
+  }
+  return x ? top_level(x) : -1;
+}
 
 template <class Pred>
 __device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) {
@@ -175,6 +225,15 @@ struct TreeShared {
   int gcount;
   int gwrite;
   int gneed;  // detached chains undecided before the chains' sort
+  // per dim g: last level of the chains of the call's present points with
+  // marker g (-1: none), in the call's tree (pst) and after restrict(D) (cst)
+  int pst[kMaxDims];
+  int cst[kMaxDims];
+  unsigned long long remc;   // levels of the restricted tree
+  unsigned long long cmask;  // dims g with cst[g] >= 0
+  unsigned long long nmask;  // dims whose chains of unmatched points can stay as phantoms
+  int kph;                   // deepest level above D's whose dim is > D (-1: none)
+  int lph;                   // a merge loses the absorbed points of leaves the first cell left empty
 };
 
 // leaf key of point x: its cells on the remaining dims (in level order, most
@@ -263,29 +322,70 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
   __syncthreads();
   for (int j = threadIdx.x; j < np; j += blockDim.x)
     if (!GUARD_OK(a.guard, P[j] >= 0 && P[j] < a.n, 53, P[j])) s.gcount = 1;
-  for (int j = threadIdx.x; j < ng; j += blockDim.x)
-    if (!GUARD_OK(a.guard, Gh[j].x >= 0 && Gh[j].x < a.n && Gh[j].y >= 0 && Gh[j].y < d, 54, Gh[j].x)) s.gcount = 1;
+  for (int j = threadIdx.x; j < ng; j += blockDim.x) {
+    const int y = Gh[j].y;
+    if (!GUARD_OK(a.guard, Gh[j].x >= 0 && Gh[j].x < a.n && y >= 0 && (y & 255) < d && (y >> 8) < d, 54, Gh[j].x))
+      s.gcount = 1;
+  }
   __syncthreads();
   if (s.gcount) return;
-  // 1. cell counts and s-connection flags on D
+  // 1. the levels of the call's tree and of the restricted one, and where the
+  //    chains of present points end in each
+  const int pD = a.lvl_pos[D];
+  const unsigned long long gtD = a.gt_pos[D];
+  if (threadIdx.x == 0) {
+    unsigned long long remp = 0;
+    for (int k = 0; k < d; ++k)
+      if (!((C.rmask >> k) & 1ull)) remp |= 1ull << a.lvl_pos[k];
+    const unsigned long long remc = remp & ~(1ull << pD);
+    s.remc = remc;
+    const unsigned long long above = remp & gtD & level_span(0, pD - 1);
+    s.kph = above ? top_level(above) : -1;
+    // restricting the deepest level: the level above keeps count-0 leaves
+    // when its dim is > D, and with no level left the root is the leaf
+    s.lph = top_level(remp) == pD && (remc == 0ull || a.lvl_dim[top_level(remc)] > D);
+  }
+  if (threadIdx.x < d) {
+    const int g = threadIdx.x;
+    int pt = -1, ct = -1;
+    if (!((C.rmask >> g) & 1ull)) {
+      // a chain starts whole at the build (ScyTreeNode.cu:36-47); present
+      // points matched every restriction, made in ascending dim order
+      const int pg = a.lvl_pos[g];
+      unsigned long long rem = d == 64 ? ~0ull : ((1ull << d) - 1ull);
+      pt = d - 1;
+      unsigned long long rm = C.rmask;
+      while (rm && pt >= 0) {
+        const int e = __ffsll((long long)rm) - 1;
+        rm &= rm - 1;
+        rem &= ~(1ull << a.lvl_pos[e]);
+        pt = chain_cut(pg, pt, a.lvl_pos[e], rem, a.gt_pos[e], true);
+      }
+      if (pt >= 0 && g != D) ct = chain_cut(pg, pt, pD, rem & ~(1ull << pD), gtD, true);
+    }
+    s.pst[g] = pt;
+    s.cst[g] = ct;
+  }
+  // 2. cell counts and s-connection flags on D
   for (int i = threadIdx.x; i < a.cells; i += blockDim.x) {
     s.cnt[i] = 0;
     s.sf[i] = 0;
   }
   __syncthreads();
+  const bool sconn_present = s.pst[D] >= 0;
   for (int j = threadIdx.x; j < np; j += blockDim.x) {
     int x = P[j];
     int c = a.cc[(size_t)x * d + D];
     atomicAdd(&s.cnt[c], 1);
-    if ((a.gz[x] >> D) & 1ull) s.sf[c] = 1;
+    if (sconn_present && ((a.gz[x] >> D) & 1ull)) s.sf[c] = 1;
   }
   for (int j = threadIdx.x; j < ng; j += blockDim.x) {
     int2 g = Gh[j];
-    if (g.y == D) s.sf[a.cc[(size_t)g.x * d + D]] = 1;
+    if ((g.y & 255) == D) s.sf[a.cc[(size_t)g.x * d + D]] = 1;
   }
   __syncthreads();
-  // 2. merge runs (InscyNodeCpu.cu:179-192 with mergeWithNeighbors) and the
-  //    remaining dims of the restricted tree
+  // 3. merge runs (InscyNodeCpu.cu:179-192 with mergeWithNeighbors) and the
+  //    remaining dims of the restricted tree, in level order
   if (threadIdx.x == 0) {
     int nr = 0, c = 0;
     while (c < a.cells) {
@@ -298,34 +398,45 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
     }
     s.nruns = nr;
     int nl = 0;
-    for (int k = 0; k < d; ++k)
-      if (!((smask >> k) & 1ull)) s.lam[nl++] = k;
+    for (int t = 0; t < d; ++t)
+      if ((s.remc >> t) & 1ull) s.lam[nl++] = a.lvl_dim[t];
     s.nlam = nl;
+    unsigned long long cm = 0, nm = 0;
+    for (int g = 0; g < d; ++g) {
+      if (s.cst[g] >= 0) cm |= 1ull << g;
+      // an unmatched point's chain stays only through a level above D's
+      // whose dim is > D
+      if (g != D && s.pst[g] >= 0 && s.kph >= 0 && a.lvl_pos[g] <= s.kph) nm |= 1ull << g;
+    }
+    s.cmask = cm;
+    s.nmask = nm;
   }
   __syncthreads();
   const int nruns = s.nruns;
   const int nlam = s.nlam;
-  const bool last_dim = (C.nrestricted + 1 == d);
   const int key_bits = (nlam + 1) * b;
+  const unsigned long long remc = s.remc;
+  const int kph = s.kph;
+  const bool lph = s.lph != 0;
   uint64_t lammask = ~smask;
   if (d < 64) lammask &= (1ull << d) - 1;
+  const Key cellmask = ((Key)1 << b) - (Key)1;
+  // trie level of dim g in the restricted tree
+  auto level_of = [&](int g) { return __popcll(remc & ((1ull << a.lvl_pos[g]) - 1ull)); };
 
   for (int r = 0; r < nruns; ++r) {
     const int c0 = s.runs[r][0], c1 = s.runs[r][1];
-    const bool drop = last_dim && c1 > c0 && s.cnt[c0] == 0;
-    // 3. restrict (+ merge): points of the run, in the parent's order
-    int m = 0;
-    if (!drop)
-      m = block_filter(
-          P, np,
-          [&](int x) {
-            int c = a.cc[(size_t)x * d + D];
-            return c >= c0 && c <= c1;
-          },
-          A, s.sh);
+    // 4. restrict (+ merge): points of the run, in the parent's order
+    int m = block_filter(
+        P, np,
+        [&](int x) {
+          int c = a.cc[(size_t)x * d + D];
+          return c >= c0 && c <= c1;
+        },
+        A, s.sh);
     for (int j = threadIdx.x; j < m; j += blockDim.x) KA[j] = leaf_key<Key>(a.cc, d, s.lam, nlam, D, b, A[j]);
     __syncthreads();
-    // 4. merged runs: stable re-sort by the leaf key (remaining cells, cell on
+    // 5. merged runs: stable re-sort by the leaf key (remaining cells, cell on
     //    D); equal keys keep their order (the restricted dims, then id)
     Key* kcur = KA;
     int* cur = A;
@@ -342,7 +453,10 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
         oth = t;
       }
     }
-    // 5. prune: weak density of the subspace, survivor prefix counts
+    // 6. prune: weak density of the subspace, survivor prefix counts.  A
+    //    merge into a leaf node that the run's first cell left empty loses
+    //    the absorbed points: they count as pruned.
+    const bool drops = lph && c1 > c0;
     int npp = 0;
     for (int c = 0; c < m; c += blockDim.x) {
       int j = c + threadIdx.x;
@@ -350,6 +464,11 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       if (j < m) {
         int x = cur[j];
         f = (wd[x >> 5] >> (x & 31)) & 1u;
+        if (f && drops) {
+          int glo, ghi;
+          key_range(kcur, m, kcur[j], b, glo, ghi);  // the point's leaf node
+          if ((int)(kcur[glo] & cellmask) != c0) f = 0;
+        }
       }
       int tot;
       int inc = block_inclusive_scan<int>(f, s.sh, &tot);
@@ -379,21 +498,24 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
           if (SV[j + 1] != SV[j]) a.out_pts[pts_off + SV[j]] = x;
         }
       }
-      // 6. ghosts of the pruned tree.  A detached chain's fate mostly follows
+      // 7. ghosts of the pruned tree.  A detached chain's fate mostly follows
       //    from the points' nodes (range searches on the sorted point keys);
       //    only a chain whose sibling node holds no point at all needs "does
       //    a deeper chain pass this node", a range search on the chains' own
       //    keys, so the region's chains are sorted by leaf key only when
       //    some chain needs that.
       int ngp = 0;
-      if (ng > 0 && !drop) {
+      if (ng > 0) {
         for (int c = 0; c < ng; c += blockDim.x) {
           int j = c + threadIdx.x;
           int f = 0;
           if (j < ng) {
             int2 gg = Gh[j];
-            int cx = a.cc[(size_t)gg.x * d + D];
-            f = (gg.y != D && gg.y >= 0 && gg.y < d && ((lammask >> gg.y) & 1ull) && cx >= c0 && cx <= c1) ? 1 : 0;
+            const int g = gg.y & 255;
+            if (g != D && ((lammask >> g) & 1ull)) {
+              const int cx = a.cc[(size_t)gg.x * d + D];
+              f = chain_cut(a.lvl_pos[g], gg.y >> 8, pD, remc, gtD, cx >= c0 && cx <= c1) >= 0 ? 1 : 0;
+            }
           }
           int tot;
           int inc = block_inclusive_scan<int>(f, s.sh, &tot);
@@ -415,16 +537,18 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
         s.gneed = 0;
       }
       __syncthreads();
-      // (a) chains of points pruned here: a chain survives when a kept point
-      //     shares the cells of every remaining dim up to the chain's
+      // (a) chains of points pruned (or lost) here: a chain survives when a
+      //     kept point shares the cells of every remaining dim up to the
+      //     chain's level
+      const unsigned long long cmask = s.cmask;
       for (int j = threadIdx.x; j < m; j += blockDim.x) {
         unsigned long long km = 0;
         if (SV[j + 1] == SV[j]) {
-          unsigned long long gb = a.gz[cur[j]] & lammask;
+          unsigned long long gb = a.gz[cur[j]] & lammask & cmask;
           while (gb) {
             const int g = __ffsll((long long)gb) - 1;
             gb &= gb - 1;
-            const int l = __popcll(lammask & ((1ull << g) - 1));
+            const int l = level_of(g);
             int plo, phi;
             key_range(kcur, m, kcur[j], b * (nlam - l), plo, phi);  // prefix through level l
             if (SV[phi] - SV[plo] > 0) km |= 1ull << g;
@@ -437,9 +561,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       //     chains are sorted (`sorted` false)
       auto decide = [&](int jj, bool sorted) -> int {
         const int2 gg = Gh[GA[jj]];
-        const int g = gg.y;
+        const int g = gg.y & 255;
         const Key kx = KG[jj];
-        const int l = __popcll(lammask & ((1ull << g) - 1));
+        const int l = level_of(g);
         int plo, phi;
         if (l > 0) {
           key_range(kcur, m, kx, b * (nlam - l + 1), plo, phi);  // prefix through level l-1: the parent node
@@ -448,12 +572,38 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
         key_range(kcur, m, kx, b * (nlam - l), plo, phi);
         if (SV[phi] - SV[plo] > 0) return 1;  // the sibling node keeps points
         if (phi > plo) return 0;              // the sibling node existed and is erased with it
+        if (a.lvl_pos[g] <= kph) {
+          // restrict kept the path of every point of the call down to level
+          // kph, so the sibling node existed (as a phantom) when a point of
+          // the call shares its cells; the call's points are in leaf order,
+          // whose first levels are these
+          const uint8_t* rx = a.cc + (size_t)gg.x * d;
+          Key want = 0;
+          for (int t = 0; t <= l; ++t) want = (want << b) | (Key)rx[s.lam[t]];
+          int lo2 = 0, hi2 = np;
+          Key got = 0;
+          while (lo2 < hi2) {
+            const int mid = (lo2 + hi2) >> 1;
+            const uint8_t* ry = a.cc + (size_t)P[mid] * d;
+            Key ky = 0;
+            for (int t = 0; t <= l; ++t) ky = (ky << b) | (Key)ry[s.lam[t]];
+            if (ky < want)
+              lo2 = mid + 1;
+            else
+              hi2 = mid;
+          }
+          if (lo2 < np) {
+            const uint8_t* ry = a.cc + (size_t)P[lo2] * d;
+            for (int t = 0; t <= l; ++t) got = (got << b) | (Key)ry[s.lam[t]];
+            if (got == want) return 0;
+          }
+        }
         // the sibling node exists only if a deeper detached chain passes it
         if (!sorted) return 2;
         int glo, ghi;
         key_range(KG, ngp, kx, b * (nlam - l), glo, ghi);
         for (int t = glo; t < ghi; ++t)
-          if (__popcll(lammask & ((1ull << Gh[GA[t]].y) - 1)) > l) return 0;
+          if (level_of(Gh[GA[t]].y & 255) > l) return 0;
         return 1;
       };
       for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) {
@@ -488,9 +638,41 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
         for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) gkeep[jj] = decide(jj, true);
         __syncthreads();
       }
+      // (c) chains of the call's points outside the run: restrict kept their
+      //     path down to level kph (phantom nodes, no points), so their
+      //     sibling node existed; a chain survives when a kept point shares
+      //     the cells up to its level.  Counted here, written below.
+      const unsigned long long nmask = s.nmask;
+      auto unmatched = [&](int j, bool write) {
+        const int x = P[j];
+        unsigned long long gb = a.gz[x] & nmask;
+        if (!gb) return 0;
+        const int cx = a.cc[(size_t)x * d + D];
+        if (cx >= c0 && cx <= c1) return 0;
+        const Key kx = leaf_key<Key>(a.cc, d, s.lam, nlam, D, b, x);
+        int kept = 0;
+        while (gb) {
+          const int g = __ffsll((long long)gb) - 1;
+          gb &= gb - 1;
+          const int pt = chain_cut(a.lvl_pos[g], s.pst[g], pD, remc, gtD, false);
+          if (pt < 0) continue;
+          const int l = level_of(g);
+          int plo, phi;
+          key_range(kcur, m, kx, b * (nlam - l), plo, phi);
+          if (SV[phi] - SV[plo] == 0) continue;
+          ++kept;
+          if (write) {
+            const int o = atomicAdd(&s.gwrite, 1);
+            if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(x, g | (pt << 8));
+          }
+        }
+        return kept;
+      };
       {
         int kept = 0;
         for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x) kept += gkeep[jj];
+        if (nmask)
+          for (int j = threadIdx.x; j < np; j += blockDim.x) kept += unmatched(j, false);
         if (kept) atomicAdd(&s.gcount, kept);
       }
       __syncthreads();
@@ -511,14 +693,20 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
             const int g = __ffsll((long long)km) - 1;
             km &= km - 1;
             const int o = atomicAdd(&s.gwrite, 1);
-            if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(cur[j], g);
+            if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(cur[j], g | (s.cst[g] << 8));
           }
         }
         for (int jj = threadIdx.x; jj < ngp; jj += blockDim.x)
           if (gkeep[jj]) {
+            const int2 gg = Gh[GA[jj]];
+            const int g = gg.y & 255;
+            const int cx = a.cc[(size_t)gg.x * d + D];
+            const int pt = chain_cut(a.lvl_pos[g], gg.y >> 8, pD, remc, gtD, cx >= c0 && cx <= c1);
             const int o = atomicAdd(&s.gwrite, 1);
-            if (o < s.gcount) a.out_ghosts[s.goff + o] = Gh[GA[jj]];
+            if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(gg.x, g | (pt << 8));
           }
+        if (nmask)
+          for (int j = threadIdx.x; j < np; j += blockDim.x) unmatched(j, true);
       }
       ghost_off = s.goff;
       nghost = s.gcount;
@@ -584,6 +772,11 @@ void launch_tree_level(const TreeLaunch& L, cudaStream_t s) {
   a.pts_in_total = L.pts_in_total;
   a.ghosts_in_total = L.ghosts_in_total;
   a.guard = L.guard;
+  for (int k = 0; k < kMaxDims; ++k) {
+    a.lvl_pos[k] = L.lvl_pos[k];
+    a.lvl_dim[k] = L.lvl_dim[k];
+    a.gt_pos[k] = L.gt_pos[k];
+  }
   if (L.key_bytes <= 4)
     tree_launches<uint32_t>(a, L, s);
   else if (L.key_bytes <= 8)

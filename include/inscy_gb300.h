@@ -31,7 +31,7 @@ enum {
   INSCY_OK = 0,
   INSCY_ERR_ARG = 1,         /* bad argument (null pointer, n < 0, d out of range, values outside [0,1]) */
   INSCY_ERR_CUDA = 2,        /* a CUDA call failed (no device, out of memory, launch failure) */
-  INSCY_ERR_UNSUPPORTED = 3, /* option not implemented (entropy_order != 0) */
+  INSCY_ERR_UNSUPPORTED = 3, /* option not implemented (no option returns it at present) */
   INSCY_ERR_LIMIT = 4,       /* input beyond a documented limit (d > 64, ceil(1/eps) > 256, cells > 255) */
   INSCY_ERR_INTERNAL = 5     /* a device-side consistency check failed */
 };
@@ -45,7 +45,8 @@ typedef struct inscy_params {
   float r;                 /* redundancy factor */
   int number_of_cells;     /* grid cells per dimension of the SCY-tree */
   int rectangular;         /* 0: phi density (ClusteringCpu.cu:166-176); 1: neighbour count (:178-183) */
-  int entropy_order;       /* dim order of the tree (inscy_map.cpp:61-121); only 0 is supported */
+  int entropy_order;       /* level order of the trees (inscy_map.cpp:61-121): 0 identity, -1 by
+                              descending cell entropy, any other value by ascending entropy */
 } inscy_params;
 
 /* Execution form of inscy_run_batch.  PLAIN: the datasets one after another.

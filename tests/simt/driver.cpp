@@ -15,7 +15,7 @@ long long launches();
 
 int main(int argc, char** argv) {
   if (argc < 12) {
-    std::fprintf(stderr, "usage: driver X.f32 n d eps F num_obj min_size r cells rect out.bin\n");
+    std::fprintf(stderr, "usage: driver X.f32 n d eps F num_obj min_size r cells rect out.bin [entropy_order]\n");
     return 2;
   }
   const long long n = atoll(argv[2]);
@@ -28,7 +28,7 @@ int main(int argc, char** argv) {
   }
   fclose(f);
   inscy_params p{(float)atof(argv[4]), (float)atof(argv[5]), atoi(argv[6]), atoi(argv[7]), (float)atof(argv[8]),
-                 atoi(argv[9]), atoi(argv[10]), 0};
+                 atoi(argv[9]), atoi(argv[10]), argc > 12 ? atoi(argv[12]) : 0};
   inscy_result* r = nullptr;
   if (inscy_run(X.data(), n, d, &p, INSCY_MODE_PLAIN, &r) != INSCY_OK) {
     std::fprintf(stderr, "inscy_run: %s\n", inscy_last_error());

@@ -45,7 +45,6 @@ def _call(engine, X, **kw):
     (dict(neighborhood_size=0.0), _lib.INSCY_ERR_ARG),
     (dict(number_of_cells=0), _lib.INSCY_ERR_ARG),
     (dict(number_of_cells=300), _lib.INSCY_ERR_LIMIT),
-    (dict(entropy_order=1), _lib.INSCY_ERR_UNSUPPORTED),
 ])
 def test_bad_parameters_are_rejected(engine, kw, code):
     rc, h = _call(engine, np.random.default_rng(0).random((10, 3)), **kw)

@@ -29,12 +29,47 @@ def test_small_workload_matches_reference_outputs(engine, rect):
     assert stats["calls"] > 0 and stats["kernel_launches"] > 0
 
 
-@pytest.mark.parametrize("case", [c for c in family_cases() if c[2]["entropy_order"] == 0],
-                         ids=lambda c: "family%d" % c[0])
+@pytest.mark.parametrize("case", family_cases(), ids=lambda c: "family%d_e%d" % (c[0], c[2]["entropy_order"]))
 def test_family_matches_reference_outputs(engine, case):
+    # includes entropy_order 1 and -1 (permuted level orders)
     i, X, p, want = case
     got, _ = gpu_run(X, **p)
     assert_same(got, want, "family %d" % i)
+
+
+def _entropy_case(seed):
+    # per-dim distributions of different entropy (uniform, one bump, three
+    # bumps), so that the level order is a real permutation, and many points
+    # near cell edges (s-connections)
+    rng = np.random.default_rng(777000 + seed)
+    n = int(rng.integers(300, 3000))
+    d = int(rng.integers(4, 15))
+    X = np.empty((n, d), np.float32)
+    for k in range(d):
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            X[:, k] = rng.random(n)
+        elif kind == 1:
+            X[:, k] = np.clip(rng.normal(rng.random(), 0.05 + 0.2 * rng.random(), n), 0, 1)
+        else:
+            c = rng.random(3)
+            X[:, k] = np.clip(c[rng.integers(0, 3, n)] + rng.normal(0, 0.03, n), 0, 1)
+    p = dict(neighborhood_size=float(rng.choice([0.03, 0.05, 0.08, 0.12, 0.2])), F=float(rng.choice([0.5, 1.0, 2.0])),
+             num_obj=int(rng.integers(2, 8)), min_size=int(rng.integers(4, 30)), r=float(rng.choice([0.5, 1.0, 2.0])),
+             number_of_cells=int(rng.integers(2, 7)), rectangular=bool(rng.integers(0, 2)),
+             entropy_order=int(rng.choice([1, -1])))
+    return X, p
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_entropy_order_matches_oracle(engine, seed):
+    """Permuted level orders (entropy_order 1 / -1) against the oracle, plain
+    and batched mode."""
+    X, p = _entropy_case(seed)
+    want = orc.run(X, **p)
+    for mode in (_lib.MODE_PLAIN, _lib.MODE_BATCHED):
+        got, _ = gpu_run(X, mode=mode, **p)
+        assert_same(got, want, "entropy seed %d mode %d (n=%d, d=%d)" % (seed, mode, X.shape[0], X.shape[1]))
 
 
 @pytest.mark.parametrize("case", range(6))
@@ -142,8 +177,8 @@ def test_torch_binding_matches_reference_outputs(engine, rect):
             p["rectangular"], p["entropy_order"])
     assert_same(tuple(ext.run_gpu_4(torch.from_numpy(X), *args)), want, "run_gpu_4, host tensor")
     assert_same(tuple(ext.run_gpu_5(torch.from_numpy(X).cuda(), *args)), want, "run_gpu_5, device tensor")
-    with pytest.raises(RuntimeError):
-        ext.run_gpu_5(torch.from_numpy(X).cuda(), *args[:-1], 1)  # entropy_order != 0 is refused
+    want_e = orc.run(X, **dict(p, entropy_order=-1))
+    assert_same(tuple(ext.run_gpu_5(torch.from_numpy(X).cuda(), *args[:-1], -1)), want_e, "run_gpu_5, entropy_order -1")
 
 
 def test_tma_row_gather_writes_the_same_lists(engine, monkeypatch):

@@ -38,7 +38,8 @@ def simt_run(driver, X, p, reverse, tag):
     X.tofile(fx)
     n, d = X.shape
     args = [driver, fx, str(n), str(d), repr(float(p["neighborhood_size"])), repr(float(p["F"])), str(p["num_obj"]),
-            str(p["min_size"]), repr(float(p["r"])), str(p["number_of_cells"]), str(int(p.get("rectangular", 0))), fo]
+            str(p["min_size"]), repr(float(p["r"])), str(p["number_of_cells"]), str(int(p.get("rectangular", 0))), fo,
+            str(int(p.get("entropy_order", 0)))]
     env = dict(os.environ)
     env.pop("SIMT_REVERSE", None)
     if reverse:
@@ -67,6 +68,16 @@ def test_family_cases(driver):
     cases = [c for c in family_cases() if c[2]["entropy_order"] == 0][:12]
     for i, X, p, want in cases:
         assert_same(simt_run(driver, X, p, i % 2 == 1, "family%d" % i), want, "family %d" % i)
+
+
+def test_family_cases_entropy_order(driver):
+    # permuted level orders: phantom nodes, cut chains, the neighbourhood
+    # walk's partial fine-cell tests
+    cases = [c for c in family_cases() if c[2]["entropy_order"] != 0]
+    assert cases
+    for i, X, p, want in cases:
+        assert_same(simt_run(driver, X, p, i % 2 == 1, "family_e%d" % i), want,
+                    "family %d (entropy_order %d)" % (i, p["entropy_order"]))
 
 
 def test_wide_rows(driver):
