@@ -16,6 +16,8 @@ Usage:  python tests/golden/make_full.py plain batch large_d   (any subset)
   large_d  the 100,000 x 25 workload, seed 0           -> full_large_d.json
   large_d_20k  the same generator and parameters at 20,000 points (d = 25,
            cells = 5, eps = 0.02), seed 0             -> full_large_d_20k.json
+  plain_entropy  the 25,000 x 15 workload, seed 0, with entropy_order 1 and
+           -1 (permuted level orders)                 -> full_plain_entropy.json
 """
 import json
 import os
@@ -60,6 +62,12 @@ def main(which):
                       index=i) for i in BATCH_PICK]
         with open(os.path.join(HERE, "full_batch.json"), "w") as f:
             json.dump({"workload": "batch64_seed0", "entries": ents}, f)
+    if "plain_entropy" in which:
+        X = synth.make_plain(0)
+        ents = [entry("plain_seed0_e%d" % eo, X, dict(synth.PARAMS["plain"], entropy_order=eo), generator="make_plain",
+                      seed=0) for eo in (1, -1)]
+        with open(os.path.join(HERE, "full_plain_entropy.json"), "w") as f:
+            json.dump({"workload": "plain_n25000_d15_entropy", "entries": ents}, f)
     if "large_d_20k" in which:
         X = synth.make_large_d(0, n=20_000)
         out = {"workload": "large_d_n20000_d25", "entries": [entry("large_d_20k_seed0", X, dict(synth.PARAMS["large_d"]),

@@ -82,3 +82,15 @@ def test_large_d_generator_at_20000_points_matches_oracle(engine):
     X = regenerate(e)
     subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]))
     assert_digest(subs, labels, e, e["name"])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "full_plain_entropy.json")),
+                    reason="the entropy-order fixture was not made")
+@pytest.mark.parametrize("k", range(2))
+def test_plain_workload_entropy_orders_match_oracle(engine, k):
+    """The 25,000 x 15 workload with entropy_order 1 and -1: permuted SCY-tree
+    and neighbourhood-trie level orders at full size."""
+    e = full_fixture("plain_entropy")["entries"][k]
+    X = regenerate(e)
+    subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]))
+    assert_digest(subs, labels, e, e["name"])
