@@ -398,6 +398,9 @@ def main():
                                                "ms_total")},
             "run": {k: st[k] for k in ("calls", "regions", "subspaces", "levels", "candidates")},
             "commit_counters": st["replay"],
+            "autotune": {"rows_takes": int(st["rows_takes"]), "rows_blocks_per_sm": int(st["rows_blocks_per_sm"]),
+                         "note": "row-kernel launch shape measured by the engine's tuner in a warm-up run: "
+                                 "work-counter updates per warp, resident blocks per SM"},
             "clustered_subspaces": len(subs)}
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_block(_lib)

@@ -40,7 +40,9 @@ class Stats(ctypes.Structure):
                [(name, ctypes.c_longlong) for name in
                 ("density_launches_pass1", "kernel_launches", "calls", "regions", "subspaces", "candidates",
                  "levels", "h2d_bytes", "d2h_bytes")] + [("replay_counters", ctypes.c_longlong * 10), ("ms_expand", ctypes.c_double),
-                                               ("ms_commit_tail", ctypes.c_double)]
+                                               ("ms_commit_tail", ctypes.c_double),
+                                               ("rows_takes", ctypes.c_int), ("rows_blocks_per_sm", ctypes.c_int),
+                                               ("ms_tune", ctypes.c_double)]
 
     COUNTERS = ("joins", "new_entries", "label_writes", "border_writes", "superset_entries", "redundancy_points",
                 "prune_calls", "prune_points", "clusters_numbered", "border_checks")

@@ -88,6 +88,23 @@ static bool rows_tma_requested() {
   const char* e = std::getenv("INSCY_ROWS_TMA");
   return e && e[0] == '1';
 }
+
+// Launch shape of the row kernel (work-counter updates per warp that the
+// pairs-per-update chunk aims at, resident blocks per SM), measured once per
+// (device, row width) in the process: on
+// the first single-pass level with at least kTunePairs (group, query) pairs,
+// each candidate shape runs the level's pass twice (every run writes the same
+// lists) and the fastest is kept.  INSCY_ROWS_TUNE=0 keeps the default shape.
+constexpr long long kTunePairs = 100000;
+struct RowShape {
+  int takes = 0, bps = 0;  // 0: 16 updates per warp / the most the registers allow
+};
+static std::mutex g_tune_m;
+static std::map<std::pair<int, int>, RowShape> g_tuned;  // (device, slots) -> shape
+static bool rows_tune_enabled() {
+  const char* e = std::getenv("INSCY_ROWS_TUNE");
+  return !(e && e[0] == '0');
+}
 // narrowest leaf key the level kernel may use (4; raised only to test the wider forms)
 #ifndef INSCY_TREE_MIN_KEY_BYTES
 #define INSCY_TREE_MIN_KEY_BYTES 4
@@ -509,6 +526,46 @@ class Engine {
            std::vector<std::vector<int>>& out_dims, std::vector<std::vector<int>>& out_labels, inscy_stats& st);
 
  private:
+  // The row kernel's launch shape for rows of `slots` on this device (see
+  // RowShape), measured on this level's single pass when no engine of the
+  // process has measured it yet.  The statistics counters are off during the
+  // trials; each trial writes the same lists, and the caller's launch follows
+  // with the chosen shape.
+  template <class Fn>
+  void tune_rows(DensityLaunch& DL, int slots, long long pairs, cudaStream_t s, Fn& neighbours) {
+    if (!rows_tune_enabled() || pairs < kTunePairs) return;
+    {
+      std::lock_guard<std::mutex> g(g_tune_m);
+      if (g_tuned.count({device_, slots})) return;
+    }
+    unsigned long long* counters[3] = {DL.cand_counter, DL.list_counter, DL.out_counter};
+    DL.cand_counter = DL.list_counter = DL.out_counter = nullptr;
+    const int bmax = rows_max_blocks_per_sm(slots);
+    std::vector<RowShape> cands = {{4, 0}, {8, 0}, {16, 0}, {32, 0}, {64, 0}};
+    if (bmax > 2) {
+      cands.push_back({16, bmax - 1});
+      cands.push_back({64, bmax - 1});
+    }
+    std::vector<double> best(cands.size(), 1e30);
+    for (int rep = 0; rep < 2; ++rep)
+      for (size_t i = 0; i < cands.size(); ++i) {
+        DL.rows_takes = cands[i].takes;
+        DL.rows_bps = cands[i].bps;
+        const double ms = timed(s, [&] { neighbours(true); });
+        stats_.ms_tune += ms;
+        best[i] = std::min(best[i], ms);
+      }
+    size_t pick = 0;
+    for (size_t i = 1; i < cands.size(); ++i)
+      if (best[i] < best[pick]) pick = i;
+    DL.rows_takes = cands[pick].takes;
+    DL.rows_bps = cands[pick].bps;
+    DL.cand_counter = counters[0];
+    DL.list_counter = counters[1];
+    DL.out_counter = counters[2];
+    std::lock_guard<std::mutex> g(g_tune_m);
+    g_tuned.emplace(std::make_pair(device_, slots), cands[pick]);
+  }
   // timing helper: device time of the work queued by f()
   template <class Fn>
   double timed(cudaStream_t s, Fn f) {
@@ -1019,6 +1076,13 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
       DL.phi_work = dphiwork;
       DL.sms = sms_;
       DL.rows_tma = rows_tma ? 1 : 0;
+      {
+        std::lock_guard<std::mutex> g(g_tune_m);
+        auto it = g_tuned.find({device_, slots});
+        const RowShape sh = it != g_tuned.end() && rows_tune_enabled() ? it->second : RowShape();
+        DL.rows_takes = sh.takes;
+        DL.rows_bps = sh.bps;
+      }
       auto neighbours = [&](bool write) {
         if (level == 1) {
           launch_neighbours(DL, write, s);
@@ -1078,6 +1142,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
           DL.cap_loff = dloff;
           DL.ent = lent;
           DL.total = L;
+          if (level > 1 && DL.work && !rows_tma) tune_rows(DL, slots, ngroup_warps, s, neighbours);
           const double ms1 = timed(s, [&] { neighbours(true); });
           stats_.ms_density += ms1;
           stats_.ms_density_pass1 += ms1;
@@ -1617,6 +1682,13 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   stats_.ms_expand = std::chrono::duration<double, std::milli>(t_expanded - t_start).count();
   committer.join();
   stats_.ms_commit_tail = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_expanded).count();
+  if (slots) {
+    std::lock_guard<std::mutex> g(g_tune_m);
+    auto it = g_tuned.find({device_, slots});
+    const RowShape sh = it != g_tuned.end() && rows_tune_enabled() ? it->second : RowShape();
+    stats_.rows_takes = sh.takes > 0 ? sh.takes : 16;
+    stats_.rows_blocks_per_sm = sh.bps > 0 ? sh.bps : rows_max_blocks_per_sm(slots);
+  }
   if (commit_err) std::rethrow_exception(commit_err);
   stats_.ms_replay_prune = t_prune_;
   stats_.ms_replay_cluster = t_cluster_;

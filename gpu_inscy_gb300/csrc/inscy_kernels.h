@@ -76,6 +76,8 @@ struct DensityLaunch {
   unsigned long long* phi_work;     // scratch of the phi kernels (kPhiWorkBytes, zeroed by the caller before each launch)
   int sms;                          // SMs of the device: persistent grids fill each once
   int rows_tma;                     // levels >= 2, d <= 32: gather the candidate rows with TMA (k_neighbours_rows_tma)
+  int rows_takes;                   // row kernel: work-counter updates per warp the chunk aims at (0: 16)
+  int rows_bps;                     // row kernel: resident blocks per SM (0: the most its registers allow)
   long long prev_total;
   long long total;
   long long prev_nkeep;
@@ -91,6 +93,8 @@ void launch_list_capacity(const DensityLaunch& L, long long nwarps, long long* c
 void launch_level1_capacity(const DensityLaunch& L, long long* cap, cudaStream_t s);
 void launch_phi_selftest(unsigned long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
 void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool write, cudaStream_t s);
+// resident blocks per SM the row kernel's registers allow (rows of `slots`)
+int rows_max_blocks_per_sm(int slots);
 void launch_keep_counts(const int* cnt, const uint8_t* flags, long long nitems, int* kcnt, int* kflag,
                         cudaStream_t s);
 void launch_keep_compact(const SubDesc* subs, int nsubs, long long nitems, const uint8_t* flags, const int* cnt,

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbours_multi(DensityArgs a) {
 // resident blocks per SM: 64 registers a thread for 16-slot rows, 85 for 24
 // and 32
 constexpr int rows_blocks_per_sm(int slots) { return slots == 16 ? 4 : 3; }
+int rows_max_blocks_per_sm(int slots) { return rows_blocks_per_sm(slots); }
 
 // kMode: 0 count, 1 write at the counted offsets (loff), 2 single-pass write
 // at capacity offsets (cap_base)
@@ -1295,9 +1296,13 @@ void launch_neighbours_multi(const DensityLaunch& L, long long nwarps, bool writ
   if (L.xrow && L.win && L.work && L.items && (L.slots == 16 || L.slots == 24 || L.slots == 32) && L.d <= L.slots) {
     // persistent warps: a grid that fills every SM once, (group, query) pairs
     // handed out by the work counter, several per update when there are many
-    const long long max_blocks = (long long)(L.sms > 0 ? L.sms : 1) * rows_blocks_per_sm(L.slots);
-    long long chunk = nwarps / (max_blocks * 8 * 16);
-    a.chunk = (int)(chunk < 1 ? 1 : chunk > 8 ? 8 : chunk);
+    const int bps_max = rows_blocks_per_sm(L.slots);
+    const int bps = L.rows_bps > 0 && L.rows_bps < bps_max ? L.rows_bps : bps_max;
+    const long long max_blocks = (long long)(L.sms > 0 ? L.sms : 1) * bps;
+    // pairs per counter update: about `takes` updates per warp over the launch
+    const long long takes = L.rows_takes > 0 ? L.rows_takes : 16;
+    long long chunk = nwarps / (max_blocks * 8 * takes);
+    a.chunk = (int)(chunk < 1 ? 1 : chunk > 64 ? 64 : chunk);
     const long long need = (nwarps + 7) / 8;
     const unsigned blocks = (unsigned)(need < max_blocks ? need : max_blocks);
     const int mode = write ? (L.cap_base ? 2 : 1) : 0;

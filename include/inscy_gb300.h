@@ -86,6 +86,14 @@ typedef struct inscy_stats {
   long long replay_counters[10];
   double ms_expand;       /* wall time of the expansion (the GPU-driving thread) */
   double ms_commit_tail;  /* time the run waited for the commit once the expansion was done */
+  /* launch shape of the candidate pass's row kernel (d <= 32): work-counter
+   * updates per warp that the pairs-per-update chunk aims at, and resident
+   * blocks per SM, chosen by the engine's tuner (measured once per row width
+   * and device in the process, on the first level with enough pairs), and the
+   * device time of the tuner's trial launches in this run */
+  int rows_takes;
+  int rows_blocks_per_sm;
+  double ms_tune;
 } inscy_stats;
 
 /* Replaces run_gpu_5 / run_gpu_4 (inscy_map.cpp:1070-1158 / :979-1067).

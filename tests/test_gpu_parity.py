@@ -277,3 +277,16 @@ def test_wide_neighbourhood_many_s_connections(engine):
         p = dict(neighborhood_size=0.3, F=1.0, num_obj=6, min_size=5, r=1.0, number_of_cells=6)
         got, _ = gpu_run(X, **p)
         assert_same(got, orc.run(X, **p), "wide eps seed %d" % seed)
+
+
+def test_row_kernel_tuner_keeps_the_lists(engine, monkeypatch):
+    """The engine's tuner picks the row kernel's launch shape by timing trial
+    launches on a large level; the chosen shape is reported, and a run without
+    the tuner gives the same labels."""
+    X = synth.make_plain(5, n=12000)
+    p = dict(synth.PARAMS["plain"])
+    got, st = gpu_run(X, **p)
+    assert st["rows_blocks_per_sm"] > 0 and st["rows_takes"] > 0
+    monkeypatch.setenv("INSCY_ROWS_TUNE", "0")
+    got0, _ = gpu_run(X, **p)
+    assert_same(got, (got0[0], got0[1]), "tuned vs default launch shape")
