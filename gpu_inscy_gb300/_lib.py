@@ -22,7 +22,8 @@ MODE_BATCHED = 1
 
 # every symbol include/inscy_gb300.h declares
 EXPORTS = ["inscy_run", "inscy_run_device", "inscy_run_batch", "inscy_run_batch_scheduled", "inscy_result_count", "inscy_result_n",
-           "inscy_result_subspace", "inscy_result_labels", "inscy_result_labels_ptr", "inscy_result_stats",
+           "inscy_result_subspace", "inscy_result_labels", "inscy_result_labels_ptr", "inscy_result_subspaces",
+           "inscy_result_label_blocks", "inscy_result_label_block", "inscy_result_label_slots", "inscy_result_stats",
            "inscy_result_free", "inscy_last_error", "inscy_version", "inscy_selftest", "inscy_selftest_noalloc",
            "inscy_mlp_params", "inscy_mlp_train", "inscy_mlp_predict", "inscy_mlp_grad", "inscy_mlp_last_error"]
 
@@ -92,6 +93,11 @@ def load():
     lib.inscy_result_labels.argtypes = [vp, c_int, vp]
     lib.inscy_result_labels_ptr.argtypes = [vp, c_int]
     lib.inscy_result_labels_ptr.restype = vp
+    lib.inscy_result_subspaces.argtypes = [vp, vp, c_int, vp]
+    lib.inscy_result_label_blocks.argtypes = [vp, ctypes.POINTER(c_int)]
+    lib.inscy_result_label_block.argtypes = [vp, c_int]
+    lib.inscy_result_label_block.restype = vp
+    lib.inscy_result_label_slots.argtypes = [vp, vp]
     lib.inscy_selftest.argtypes = [i64]
     lib.inscy_selftest.restype = i64
     lib.inscy_selftest_noalloc.argtypes = [i64, vp]
@@ -128,11 +134,11 @@ class _Owner:
 
 
 class _View:
-    """numpy view of one label vector inside a result (no copy)."""
+    """numpy view of a block of label rows inside a result (no copy)."""
 
-    def __init__(self, owner, ptr, n):
+    def __init__(self, owner, ptr, rows, n):
         self.owner = owner
-        self.__array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, True), "version": 3}
+        self.__array_interface__ = {"shape": (rows, n), "typestr": "<i4", "data": (ptr, True), "version": 3}
 
 
 def collect(handle):
@@ -140,18 +146,35 @@ def collect(handle):
 
     `labels` is a list of int32 arrays of length n, one per clustered
     subspace, viewing the result's memory (freed when the last view dies).
+    The result is read in a few calls: all subspaces at once, the label
+    blocks as 2-d views, and each subspace's row of them.
     """
     lib = load()
     owner = _Owner(handle)
     k = lib.inscy_result_count(handle)
     n = lib.inscy_result_n(handle)
-    dims = np.zeros(64, np.int32)
     subspaces, labels = [], []
-    for i in range(k):
-        m = lib.inscy_result_subspace(handle, i, dims.ctypes.data, 64)
-        subspaces.append([int(x) for x in dims[:m]])
-        ptr = lib.inscy_result_labels_ptr(handle, i)
-        labels.append(np.asarray(_View(owner, ptr, n)) if n else np.empty(0, np.int32))
+    if k > 0:
+        lens = np.zeros(k, np.int32)
+        flat = np.zeros(64 * k, np.int32)
+        w = lib.inscy_result_subspaces(handle, flat.ctypes.data, flat.size, lens.ctypes.data)
+        if w < 0:
+            raise RuntimeError("inscy_result_subspaces failed")
+        fl, o = flat[:w].tolist(), 0
+        for m in lens.tolist():
+            subspaces.append(fl[o:o + m])
+            o += m
+        if n:
+            rows = ctypes.c_int(0)
+            nb = lib.inscy_result_label_blocks(handle, ctypes.byref(rows))
+            blocks = [np.asarray(_View(owner, lib.inscy_result_label_block(handle, b), rows.value, n))
+                      for b in range(nb)]
+            slots = np.zeros(k, np.int32)
+            check(lib.inscy_result_label_slots(handle, slots.ctypes.data))
+            r = rows.value
+            labels = [blocks[s // r][s % r] for s in slots.tolist()]
+        else:
+            labels = [np.empty(0, np.int32) for _ in range(k)]
     st = Stats()
     check(lib.inscy_result_stats(handle, ctypes.byref(st)))
     return subspaces, labels, st.as_dict()

@@ -289,10 +289,37 @@ struct Phase {
   std::vector<HSub> subs;      // its clustered subspaces
 };
 
+// The label vectors of a run's result-map entries: rows of n ints in blocks
+// of `rows` rows (about 32 MB a block), taken in the order the entries are
+// created.  A result hands them over as a few 2-d arrays and one slot per
+// clustered subspace, so a binding builds its label views without a call
+// per subspace.
+struct LabelBlocks {
+  long long n = 0;
+  int rows = 1;  // rows per block
+  int used = 0;  // rows taken
+  std::vector<std::unique_ptr<int[]>> blocks;
+  void reset(long long points) {
+    n = points;
+    const long long per = (32LL << 20) / (4 * std::max(1LL, points));
+    rows = (int)std::max(1LL, std::min(256LL, per));
+    used = 0;
+    blocks.clear();
+  }
+  // a new row (uninitialised) and its slot
+  int* take(int& slot) {
+    if (used == (int)blocks.size() * rows) blocks.emplace_back(new int[(size_t)rows * (size_t)n]);
+    slot = used++;
+    return row(slot);
+  }
+  int* row(int slot) const { return blocks[slot / rows].get() + (size_t)(slot % rows) * (size_t)n; }
+};
+
 // One result-map entry (a clustered subspace) during the commit.
 struct Entry {
   uint64_t mask = 0;
-  std::vector<int> lab;        // one label per point (-1 noise, -2 border)
+  int* lab = nullptr;          // one label per point (-1 noise, -2 border): a row of the run's LabelBlocks
+  int slot = -1;               // that row
   std::vector<int> size;       // points per label (index = label)
   std::vector<LabelRef> src;   // members of each label (may include points relabelled since)
   int maxv = -100000;          // v_max(lab) (util.cu:566-574)
@@ -523,7 +550,8 @@ class Engine {
   }
 
   void run(const float* X, bool on_device, long long n, int d, const HostParams& hp, cudaStream_t s,
-           std::vector<std::vector<int>>& out_dims, std::vector<std::vector<int>>& out_labels, inscy_stats& st);
+           std::vector<std::vector<int>>& out_dims, LabelBlocks& out_labels, std::vector<int>& out_slots,
+           inscy_stats& st);
 
  private:
   // The row kernel's launch shape for rows of `slots` on this device (see
@@ -631,6 +659,7 @@ class Engine {
   std::vector<Phase> phases_;  // ranges of first restricted dims
   std::vector<int> phase_of_;  // phase of every first restricted dim
   std::vector<std::unique_ptr<Entry>> ents_;  // result map entries, in insertion order
+  LabelBlocks labs_;                           // their label vectors
   std::vector<uint64_t> emask_;               // their subspaces
   std::map<uint64_t, int> eidx_;              // subspace -> entry
   std::vector<std::vector<uint64_t>> dim_bits_;  // per dim: bitset of the entries whose subspace holds it
@@ -648,7 +677,8 @@ class Engine {
 
 // ---------------------------------------------------------------------------
 void Engine::run(const float* X, bool on_device, long long n, int d, const HostParams& hp, cudaStream_t s,
-                 std::vector<std::vector<int>>& out_dims, std::vector<std::vector<int>>& out_labels, inscy_stats& st) {
+                 std::vector<std::vector<int>>& out_dims, LabelBlocks& out_labels, std::vector<int>& out_slots,
+                 inscy_stats& st) {
   auto t_start = std::chrono::steady_clock::now();
   std::memset(&stats_, 0, sizeof(stats_));
   hp_ = hp;
@@ -662,8 +692,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
   emask_.clear();
   eidx_.clear();
   dim_bits_.assign(d, std::vector<uint64_t>());
+  labs_.reset(n);
   out_dims.clear();
-  out_labels.clear();
+  out_slots.clear();
+  out_labels.reset(n);
   if (n == 0) {
     st = stats_;
     return;
@@ -1700,9 +1732,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
     for (size_t i = 0; i < ents_.size(); ++i) order.emplace(dims_of(emask_[i]), (int)i);
     for (auto& kv : order) {
       out_dims.push_back(kv.first);
-      out_labels.push_back(std::move(ents_[kv.second]->lab));
+      out_slots.push_back(ents_[kv.second]->slot);
     }
   }
+  out_labels = std::move(labs_);
+  labs_ = LabelBlocks();
   ents_.clear();
   emask_.clear();
   eidx_.clear();
@@ -1827,7 +1861,7 @@ bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
     if (!use_bits) {
       // the entry matters only if its minimum ends above max_min, so the scan
       // stops once the minimum so far is at or below it
-      const int* lab = E.lab.data();
+      const int* lab = E.lab;
       const int* esz = E.size.data();
       int j = 0;
       for (; j < m; ++j) {
@@ -1989,7 +2023,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         const HSub& hs = *H.src[l].hs;
         const int cp = H.src[l].comp;
         const long long m = hs.moff[cp + 1] - hs.moff[cp];
-        walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, m, H.lab.data(), l, (float)hsz});
+        walk_.push_back(Walk{hs.members.data() + hs.moff[cp], 0, m, H.lab, l, (float)hsz});
         total += m;
       }
     }
@@ -2062,7 +2096,8 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
   } else {
     std::unique_ptr<Entry> ne(new Entry());
     ne->mask = smask;
-    ne->lab.assign(n_, -1);
+    ne->lab = labs_.take(ne->slot);
+    std::fill(ne->lab, ne->lab + n_, -1);
     E = ne.get();
     rc_[1]++;
     eidx_[smask] = (int)ents_.size();
@@ -2099,7 +2134,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     pieces_.push_back(Walk{hs.borders.data() + hs.boff[cp], 0, hs.boff[cp + 1] - hs.boff[cp], nullptr, -2, 0.f});
     work += hs.boff[cp + 1] - hs.boff[cp];
   }
-  int* lab = E->lab.data();
+  int* lab = E->lab;
   int* esz = E->size.data();
   if (work < kParallelWalk || hpool_->workers() == 0) {
     for (const Walk& w : pieces_) {
@@ -2158,7 +2193,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       msz = std::max(msz, E->size[l]);
     }
   if (mx == -100000) {
-    for (int v : E->lab) mx = std::max(mx, v);
+    for (long long q = 0; q < n_; ++q) mx = std::max(mx, E->lab[q]);
   }
   E->maxv = mx;
   E->maxsz = msz;
@@ -2173,7 +2208,8 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
 struct inscy_result {
   long long n = 0;
   std::vector<std::vector<int>> dims;
-  std::vector<std::vector<int>> labels;
+  inscy::LabelBlocks labels;  // label rows of the clustered subspaces
+  std::vector<int> slots;     // row of each clustered subspace, in the result map's order
   inscy_stats stats;
 };
 
@@ -2228,7 +2264,7 @@ int run_common(const float* X, bool on_device, int64_t n, int d, const inscy_par
     hp.entropy_order = p->entropy_order;
     std::unique_ptr<inscy_result> res(new inscy_result());
     res->n = n;
-    g_engine->run(X, on_device, n, d, hp, (cudaStream_t)stream, res->dims, res->labels, res->stats);
+    g_engine->run(X, on_device, n, d, hp, (cudaStream_t)stream, res->dims, res->labels, res->slots, res->stats);
     *out = res.release();
     g_err.clear();
     return INSCY_OK;
@@ -2416,8 +2452,8 @@ int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap) {
 }
 
 int inscy_result_labels(const inscy_result* r, int i, int32_t* out) {
-  if (!r || !out || i < 0 || i >= (int)r->labels.size()) return fail(INSCY_ERR_ARG, "bad result index");
-  std::memcpy(out, r->labels[i].data(), sizeof(int32_t) * r->labels[i].size());
+  if (!r || !out || i < 0 || i >= (int)r->slots.size()) return fail(INSCY_ERR_ARG, "bad result index");
+  std::memcpy(out, r->labels.row(r->slots[i]), sizeof(int32_t) * (size_t)r->n);
   return INSCY_OK;
 }
 
@@ -2452,8 +2488,36 @@ int64_t inscy_selftest(int64_t count) {
 }
 
 const int32_t* inscy_result_labels_ptr(const inscy_result* r, int i) {
-  if (!r || i < 0 || i >= (int)r->labels.size()) return nullptr;
-  return r->labels[i].data();
+  if (!r || i < 0 || i >= (int)r->slots.size()) return nullptr;
+  return r->labels.row(r->slots[i]);
+}
+
+int inscy_result_subspaces(const inscy_result* r, int32_t* dims, int cap, int32_t* lens) {
+  if (!r || !lens || (cap > 0 && !dims)) return -1;
+  int w = 0;
+  for (size_t i = 0; i < r->dims.size(); ++i) {
+    lens[i] = (int32_t)r->dims[i].size();
+    for (int v : r->dims[i])
+      if (w < cap) dims[w++] = v;
+  }
+  return w;
+}
+
+int inscy_result_label_blocks(const inscy_result* r, int* rows) {
+  if (!r) return -1;
+  if (rows) *rows = r->labels.rows;
+  return (int)r->labels.blocks.size();
+}
+
+const int32_t* inscy_result_label_block(const inscy_result* r, int b) {
+  if (!r || b < 0 || b >= (int)r->labels.blocks.size()) return nullptr;
+  return r->labels.blocks[b].get();
+}
+
+int inscy_result_label_slots(const inscy_result* r, int32_t* slots) {
+  if (!r || (!slots && !r->slots.empty())) return fail(INSCY_ERR_ARG, "NULL argument");
+  for (size_t i = 0; i < r->slots.size(); ++i) slots[i] = r->slots[i];
+  return INSCY_OK;
 }
 
 }  // extern "C"

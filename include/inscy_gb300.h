@@ -150,6 +150,18 @@ int64_t inscy_result_n(const inscy_result* r);              /* number of points 
 int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap); /* returns |S|, writes min(|S|,cap) dims */
 int inscy_result_labels(const inscy_result* r, int i, int32_t* out);        /* copies n labels */
 const int32_t* inscy_result_labels_ptr(const inscy_result* r, int i);       /* n labels, valid until free; NULL on bad i */
+/* The whole result in a few calls (no counterpart in the reference, whose
+ * binding converts to Python lists): every clustered subspace's dims, back
+ * to back, with lens[i] = |S_i| (returns the dims written, at most cap, or
+ * -1); the label vectors as blocks of `*rows` rows of n int32 each
+ * (inscy_result_label_blocks returns the block count, inscy_result_label_block
+ * the first row of block b), and the row ("slot") of each clustered
+ * subspace's labels: row s lies in block s / rows at (s % rows) * n.  All
+ * valid until inscy_result_free. */
+int inscy_result_subspaces(const inscy_result* r, int32_t* dims, int cap, int32_t* lens);
+int inscy_result_label_blocks(const inscy_result* r, int* rows);
+const int32_t* inscy_result_label_block(const inscy_result* r, int b);
+int inscy_result_label_slots(const inscy_result* r, int32_t* slots);
 int inscy_result_stats(const inscy_result* r, inscy_stats* out);
 void inscy_result_free(inscy_result* r);
 
