@@ -195,12 +195,17 @@ def batched_block(_lib):
         tried[lanes] = time.perf_counter() - t0
     lanes = min(tried, key=tried.get)
     _lib.run_batch(Xs, params, _lib.MODE_BATCHED, lanes=lanes)  # warm-up at the chosen lane count
-    t0 = time.perf_counter()
-    fifo = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, lanes=lanes)
-    t_fifo = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    lrn = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, order=learned, lanes=lanes)
-    t_learned = time.perf_counter() - t0
+    # the two schedules alternate, three runs each; the best run of each counts
+    # (one run's makespan varies by a few per cent with the host's load)
+    fifo_runs, learned_runs = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        fifo = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, lanes=lanes)
+        fifo_runs.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        lrn = _lib.run_batch(Xs, params, _lib.MODE_BATCHED, order=learned, lanes=lanes)
+        learned_runs.append(time.perf_counter() - t0)
+    t_fifo, t_learned = min(fifo_runs), min(learned_runs)
     same = all(a[0] == b[0] and a[0] == c[0] and np.array_equal(np.asarray(a[1]), np.asarray(b[1])) and
                np.array_equal(np.asarray(a[1]), np.asarray(c[1])) for a, b, c in zip(plain, fifo, lrn))
     # the datasets with oracle fixtures (tests/golden/full_batch.json)
@@ -213,6 +218,7 @@ def batched_block(_lib):
             "datasets": len(Xs), "points": points, "lanes": lanes,
             "lanes_tried_s": {str(k): round(v, 3) for k, v in tried.items()},
             "plain_s": round(sum(t_plain), 3), "fifo_s": round(t_fifo, 3), "learned_s": round(t_learned, 3),
+            "fifo_runs_s": [round(t, 3) for t in fifo_runs], "learned_runs_s": [round(t, 3) for t in learned_runs],
             "plain_points_per_s": points / sum(t_plain), "fifo_points_per_s": points / t_fifo,
             "learned_points_per_s": points / t_learned,
             "learned_vs_plain": sum(t_plain) / t_learned, "learned_vs_fifo": t_fifo / t_learned,

@@ -18,6 +18,12 @@ Usage:  python tests/golden/make_full.py plain batch large_d   (any subset)
            cells = 5, eps = 0.02), seed 0             -> full_large_d_20k.json
   plain_entropy  the 25,000 x 15 workload, seed 0, with entropy_order 1 and
            -1 (permuted level orders)                 -> full_plain_entropy.json
+  rect     rectangular density (neighbour counts, the paper's setting): the
+           25,000 x 15 workload and the 100,000 x 25 generator at 20,000
+           points, seed 0                             -> full_rect.json
+  large_d_20k_entropy  the 100,000 x 25 generator at 20,000 points with
+           entropy_order 1 (d = 25: 32-slot rows, five cells)
+                                                      -> full_large_d_20k_entropy.json
 """
 import json
 import os
@@ -68,6 +74,21 @@ def main(which):
                       seed=0) for eo in (1, -1)]
         with open(os.path.join(HERE, "full_plain_entropy.json"), "w") as f:
             json.dump({"workload": "plain_n25000_d15_entropy", "entries": ents}, f)
+    if "rect" in which:
+        ents = [entry("plain_seed0_rect", synth.make_plain(0), dict(synth.PARAMS["plain"], rectangular=True),
+                      generator="make_plain", seed=0),
+                entry("large_d_20k_seed0_rect", synth.make_large_d(0, n=20_000),
+                      dict(synth.PARAMS["large_d"], rectangular=True), generator="make_large_d", seed=0,
+                      n_arg=20_000)]
+        with open(os.path.join(HERE, "full_rect.json"), "w") as f:
+            json.dump({"workload": "rectangular", "entries": ents}, f)
+    if "large_d_20k_entropy" in which:
+        X = synth.make_large_d(0, n=20_000)
+        out = {"workload": "large_d_n20000_d25_entropy",
+               "entries": [entry("large_d_20k_seed0_e1", X, dict(synth.PARAMS["large_d"], entropy_order=1),
+                                 generator="make_large_d", seed=0, n_arg=20_000)]}
+        with open(os.path.join(HERE, "full_large_d_20k_entropy.json"), "w") as f:
+            json.dump(out, f)
     if "large_d_20k" in which:
         X = synth.make_large_d(0, n=20_000)
         out = {"workload": "large_d_n20000_d25", "entries": [entry("large_d_20k_seed0", X, dict(synth.PARAMS["large_d"]),

@@ -94,3 +94,27 @@ def test_plain_workload_entropy_orders_match_oracle(engine, k):
     X = regenerate(e)
     subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]))
     assert_digest(subs, labels, e, e["name"])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "full_rect.json")),
+                    reason="the rectangular fixture was not made")
+@pytest.mark.parametrize("k", range(2))
+def test_rectangular_density_at_full_size_matches_oracle(engine, k):
+    """rectangular=True (density by neighbour count, the paper's setting) on the
+    25,000 x 15 workload and the 100,000 x 25 generator at 20,000 points."""
+    e = full_fixture("rect")["entries"][k]
+    X = regenerate(e)
+    subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]))
+    assert_digest(subs, labels, e, e["name"])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "full_large_d_20k_entropy.json")),
+                    reason="the 20,000 x 25 entropy-order fixture was not made")
+def test_large_d_generator_entropy_order_matches_oracle(engine):
+    """entropy_order 1 on the 100,000 x 25 generator at 20,000 points (d = 25,
+    five cells: deep permuted tries, 32-slot rows), plain and batched mode."""
+    e = full_fixture("large_d_20k_entropy")["entries"][0]
+    X = regenerate(e)
+    for mode in (_lib.MODE_PLAIN, _lib.MODE_BATCHED):
+        subs, labels, _ = _lib.run_host(X, _lib.make_params(**e["params"]), mode)
+        assert_digest(subs, labels, e, e["name"] + " mode %d" % mode)
