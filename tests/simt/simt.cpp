@@ -184,7 +184,7 @@ static void run_block(unsigned b, int T) {
   std::vector<Fiber>& fib = *g_fibers;
   if ((int)fib.size() < T) fib.resize(T);
   const int nw = (T + 31) / 32;
-  g_bid = uint3{b, 0, 0};
+  g_bid = uint3{b % g_gdim.x, b / g_gdim.x, 0};  // blocks run by linear index, x fastest
   for (int t = 0; t < T; ++t) init_fiber(fib[t], (unsigned)t);
   int done = 0;
   for (;;) {
@@ -278,7 +278,7 @@ static void worker() {
 
 void launch_impl(const char* name, dim3 grid, dim3 block, CallFn fn, void* obj) {
   g_name = name;
-  if (grid.y != 1 || grid.z != 1 || block.y != 1 || block.z != 1) die("only 1-D launches are supported");
+  if (grid.z != 1 || block.y != 1 || block.z != 1) die("only 1-D blocks and 1-D or 2-D grids are supported");
   if (block.x == 0 || block.x > 1024) die("bad block size");
   ++g_launches;
   g_fn = fn;
@@ -286,8 +286,9 @@ void launch_impl(const char* name, dim3 grid, dim3 block, CallFn fn, void* obj) 
   g_gdim = grid;
   g_bdim = block;
   const int T = (int)block.x;
-  if (g_nthreads <= 1 || grid.x == 1) {
-    for (unsigned b = 0; b < grid.x; ++b) run_block(b, T);
+  const unsigned nblocks = grid.x * grid.y;
+  if (g_nthreads <= 1 || nblocks == 1) {
+    for (unsigned b = 0; b < nblocks; ++b) run_block(b, T);
   } else {
     std::unique_lock<std::mutex> lk(g_pm);
     if (!g_workers) {
@@ -295,7 +296,7 @@ void launch_impl(const char* name, dim3 grid, dim3 block, CallFn fn, void* obj) 
       for (int i = 0; i < g_nthreads; ++i) g_workers->emplace_back(worker);
       for (auto& t : *g_workers) t.detach();
     }
-    g_pgrid = grid.x;
+    g_pgrid = nblocks;
     g_pT = T;
     g_next = 0;
     g_pactive = (int)g_workers->size();
