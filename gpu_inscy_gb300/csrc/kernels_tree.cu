@@ -492,12 +492,16 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       }
       __syncthreads();
       pts_off = s.off;
-      if (pts_off >= 0) {
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-          int x = cur[j];
-          if (SV[j + 1] != SV[j]) a.out_pts[pts_off + SV[j]] = x;
+      // kpos[r]: position (in the sorted order) of the r-th kept point, in the
+      // int buffer the merge sort did not end in
+      int* kpos = cur == A ? B : A;
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        if (SV[j + 1] != SV[j]) {
+          kpos[SV[j]] = j;
+          if (pts_off >= 0) a.out_pts[pts_off + SV[j]] = cur[j];
         }
       }
+      __syncthreads();
       // 7. ghosts of the pruned tree.  A detached chain's fate mostly follows
       //    from the points' nodes (range searches on the sorted point keys);
       //    only a chain whose sibling node holds no point at all needs "does
@@ -540,18 +544,29 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       // (a) chains of points pruned (or lost) here: a chain survives when a
       //     kept point shares the cells of every remaining dim up to the
       //     chain's level
+      //     The keys are sorted, so of all kept points the nearest one on
+      //     either side of a position shares the longest prefix with it: "a
+      //     kept point shares the cells through level l" is a test of those
+      //     two.  kept_left(p): the last kept position < p; kept_right(p): the
+      //     first kept position >= p (-1: none).
+      auto kept_left = [&](int p) { return SV[p] > 0 ? kpos[SV[p] - 1] : -1; };
+      auto kept_right = [&](int p) { return SV[p] < npp ? kpos[SV[p]] : -1; };
       const unsigned long long cmask = s.cmask;
       for (int j = threadIdx.x; j < m; j += blockDim.x) {
         unsigned long long km = 0;
         if (SV[j + 1] == SV[j]) {
           unsigned long long gb = a.gz[cur[j]] & lammask & cmask;
-          while (gb) {
-            const int g = __ffsll((long long)gb) - 1;
-            gb &= gb - 1;
-            const int l = level_of(g);
-            int plo, phi;
-            key_range(kcur, m, kcur[j], b * (nlam - l), plo, phi);  // prefix through level l
-            if (SV[phi] - SV[plo] > 0) km |= 1ull << g;
+          if (gb) {
+            const Key kj = kcur[j];
+            const int il = kept_left(j), ir = kept_right(j);
+            const Key xl = il >= 0 ? kcur[il] ^ kj : ~(Key)0;
+            const Key xr = ir >= 0 ? kcur[ir] ^ kj : ~(Key)0;
+            while (gb) {
+              const int g = __ffsll((long long)gb) - 1;
+              gb &= gb - 1;
+              const int sh = b * (nlam - level_of(g));  // prefix through the chain's level
+              if ((xl >> sh) == 0 || (xr >> sh) == 0) km |= 1ull << g;
+            }
           }
           if (km) atomicAdd(&s.gcount, __popcll(km));
         }
@@ -559,19 +574,34 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       }
       // (b) chains detached earlier: 1 kept, 0 dropped, 2 undecided until the
       //     chains are sorted (`sorted` false)
+      // a key's place among the sorted point keys, and whether a kept point
+      // (kept) or any point (any) shares its prefix above bit sh
+      auto lower = [&](Key kx) {
+        int lo = 0, hi = m;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (kcur[mid] < kx)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        return lo;
+      };
+      auto kept_shares = [&](Key kx, int p, int sh) {
+        const int il = kept_left(p), ir = kept_right(p);
+        return (il >= 0 && ((kcur[il] ^ kx) >> sh) == 0) || (ir >= 0 && ((kcur[ir] ^ kx) >> sh) == 0);
+      };
       auto decide = [&](int jj, bool sorted) -> int {
         const int2 gg = Gh[GA[jj]];
         const int g = gg.y & 255;
         const Key kx = KG[jj];
         const int l = level_of(g);
-        int plo, phi;
-        if (l > 0) {
-          key_range(kcur, m, kx, b * (nlam - l + 1), plo, phi);  // prefix through level l-1: the parent node
-          if (SV[phi] - SV[plo] == 0) return 0;
-        }
-        key_range(kcur, m, kx, b * (nlam - l), plo, phi);
-        if (SV[phi] - SV[plo] > 0) return 1;  // the sibling node keeps points
-        if (phi > plo) return 0;              // the sibling node existed and is erased with it
+        const int p = lower(kx);
+        const int sh = b * (nlam - l);
+        if (l > 0 && !kept_shares(kx, p, sh + b)) return 0;  // the parent node (through level l-1) keeps no point
+        if (kept_shares(kx, p, sh)) return 1;                 // the sibling node keeps points
+        if ((p > 0 && ((kcur[p - 1] ^ kx) >> sh) == 0) || (p < m && ((kcur[p] ^ kx) >> sh) == 0))
+          return 0;  // the sibling node existed and is erased with it
         if (a.lvl_pos[g] <= kph) {
           // restrict kept the path of every point of the call down to level
           // kph, so the sibling node existed (as a phantom) when a point of
@@ -656,10 +686,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
           gb &= gb - 1;
           const int pt = chain_cut(a.lvl_pos[g], s.pst[g], pD, remc, gtD, false);
           if (pt < 0) continue;
-          const int l = level_of(g);
-          int plo, phi;
-          key_range(kcur, m, kx, b * (nlam - l), plo, phi);
-          if (SV[phi] - SV[plo] == 0) continue;
+          if (!kept_shares(kx, lower(kx), b * (nlam - level_of(g)))) continue;
           ++kept;
           if (write) {
             const int o = atomicAdd(&s.gwrite, 1);
