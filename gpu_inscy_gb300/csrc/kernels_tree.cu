@@ -149,12 +149,12 @@ __device__ int block_filter(const int* in, int n, Pred pred, int* out, int* sh) 
 // the key (warp match for the intra-warp rank, block scan across warps)
 template <int kWarps, class Key>
 __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* vout, int n, int shift, int* s_base,
-                                int* s_tot, int* s_wc) {
+                                int* s_tot, int* s_wc, int dmask = 255) {
   const int R = 256;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < R; i += blockDim.x) s_base[i] = 0;
   __syncthreads();
-  for (int j = threadIdx.x; j < n; j += blockDim.x) atomicAdd(&s_base[(int)(kin[j] >> shift) & 255], 1);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) atomicAdd(&s_base[(int)(kin[j] >> shift) & dmask], 1);
   __syncthreads();
   if (threadIdx.x < 32) {
     // exclusive scan of the 256 digit counts by one warp
@@ -182,7 +182,7 @@ __device__ void block_sort_pass(const Key* kin, const int* vin, Key* kout, int* 
     bool valid = j < n;
     Key k = valid ? kin[j] : (Key)0;
     int x = valid ? vin[j] : 0;
-    int v = valid ? ((int)(k >> shift) & 255) : R + (int)lane;
+    int v = valid ? ((int)(k >> shift) & dmask) : R + (int)lane;
     unsigned peers = __match_any_sync(0xffffffffu, v);
     int rank = __popc(peers & lanemask_lt());
     if (valid && rank == 0) s_wc[warp * R + v] = __popc(peers);
@@ -225,6 +225,7 @@ struct TreeShared {
   int gcount;
   int gwrite;
   int gneed;  // detached chains undecided before the chains' sort
+  int seg[kMaxCells + 2];  // a merged run: start of each cell's points after the partition
   // per dim g: last level of the chains of the call's present points with
   // marker g (-1: none), in the call's tree (pst) and after restrict(D) (cst)
   int pst[kMaxDims];
@@ -437,10 +438,49 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
     for (int j = threadIdx.x; j < m; j += blockDim.x) KA[j] = leaf_key<Key>(a.cc, d, s.lam, nlam, D, b, A[j]);
     __syncthreads();
     // 5. merged runs: stable re-sort by the leaf key (remaining cells, cell on
-    //    D); equal keys keep their order (the restricted dims, then id)
+    //    D); equal keys keep their order (the restricted dims, then id).  The
+    //    points of one cell come in the parent's order, which already orders
+    //    them by this key (their cell on D is the same), so a run of up to 8
+    //    cells is a stable partition by the cell on D and a merge: a point's
+    //    place is its rank in its cell plus the keys smaller than its own in
+    //    the other cells (binary searches; keys of different cells differ).
+    //    Longer runs take the radix passes over the whole key.
     Key* kcur = KA;
     int* cur = A;
-    if (c1 > c0 && m > 1) {
+    if (c1 > c0 && m > 1 && c1 - c0 < 8) {
+      block_sort_pass<kThreads / 32>(KA, A, KB, B, m, 0, s.base, s.tot, s.wc, (int)cellmask);
+      if (threadIdx.x == 0) {
+        int o = 0;
+        for (int c = c0; c <= c1; ++c) {
+          s.seg[c - c0] = o;
+          o += s.cnt[c];
+        }
+        s.seg[c1 - c0 + 1] = o;
+      }
+      __syncthreads();
+      const int nk = c1 - c0 + 1;
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const Key key = KB[i];
+        const int ci = (int)(key & cellmask) - c0;
+        int pos = i - s.seg[ci];
+        for (int t = 0; t < nk; ++t) {
+          if (t == ci) continue;
+          int lo = s.seg[t], hi = s.seg[t + 1];
+          const int base0 = lo;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (KB[mid] < key)
+              lo = mid + 1;
+            else
+              hi = mid;
+          }
+          pos += lo - base0;
+        }
+        KA[pos] = key;
+        A[pos] = B[i];
+      }
+      __syncthreads();
+    } else if (c1 > c0 && m > 1) {
       Key* koth = KB;
       int* oth = B;
       for (int sh = 0; sh < key_bits; sh += 8) {
