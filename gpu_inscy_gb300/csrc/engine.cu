@@ -1362,7 +1362,7 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
           work_scr.push_back(scr);
           // keys (16 B) of points and chains, then ints (see k_tree_level)
           long long bytes = 16LL * (2LL * F.hcalls[i].npts + 2LL * F.hcalls[i].nghost) +
-                            4LL * (3LL * F.hcalls[i].npts + 1 + 2LL * F.hcalls[i].nghost);
+                            4LL * (3LL * F.hcalls[i].npts + 1 + 3LL * F.hcalls[i].nghost);
           scr += (bytes + 15) / 16 * 16;
         }
         for (int t = 0; t < nd; ++t)

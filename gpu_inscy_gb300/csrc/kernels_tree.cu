@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
   int* SV = B + np;       // np + 1 survivor prefix counts
   int* GA = SV + np + 1;  // ng: detached chains of the region
   int* GB = GA + ng;
+  int* GC = GB + ng;      // ng: per detached chain, its cell on D and its cut (see step 2)
   RegionRec* rec = a.recs + (long long)w * a.cells;
 
   // 0. the call's points and chains must be valid ids (checked once)
@@ -380,9 +381,26 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
     atomicAdd(&s.cnt[c], 1);
     if (sconn_present && ((a.gz[x] >> D) & 1ull)) s.sf[c] = 1;
   }
-  for (int j = threadIdx.x; j < ng; j += blockDim.x) {
-    int2 g = Gh[j];
-    if ((g.y & 255) == D) s.sf[a.cc[(size_t)g.x * d + D]] = 1;
+  // per detached chain, once for all runs: its point's cell on D (bits 0-7)
+  // and its last level + 1 after the restriction when that cell is in the run
+  // (bits 8-15) and when not (bits 16-23); 0: gone (or marker on D / restricted)
+  {
+    const unsigned long long remc0 = s.remc;
+    uint64_t lm = ~smask;
+    if (d < 64) lm &= (1ull << d) - 1;
+    for (int j = threadIdx.x; j < ng; j += blockDim.x) {
+      const int2 gg = Gh[j];
+      const int g = gg.y & 255;
+      const int cx = a.cc[(size_t)gg.x * d + D];
+      if (g == D) s.sf[cx] = 1;
+      int packed = cx;
+      if (g != D && ((lm >> g) & 1ull)) {
+        const int pm = chain_cut(a.lvl_pos[g], gg.y >> 8, pD, remc0, gtD, true);
+        const int pn = chain_cut(a.lvl_pos[g], gg.y >> 8, pD, remc0, gtD, false);
+        packed |= ((pm + 1) << 8) | ((pn + 1) << 16);
+      }
+      GC[j] = packed;
+    }
   }
   __syncthreads();
   // 3. merge runs (InscyNodeCpu.cu:179-192 with mergeWithNeighbors) and the
@@ -554,12 +572,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
           int j = c + threadIdx.x;
           int f = 0;
           if (j < ng) {
-            int2 gg = Gh[j];
-            const int g = gg.y & 255;
-            if (g != D && ((lammask >> g) & 1ull)) {
-              const int cx = a.cc[(size_t)gg.x * d + D];
-              f = chain_cut(a.lvl_pos[g], gg.y >> 8, pD, remc, gtD, cx >= c0 && cx <= c1) >= 0 ? 1 : 0;
-            }
+            const int gc = GC[j];
+            const int cx = gc & 255;
+            f = ((gc >> ((cx >= c0 && cx <= c1) ? 8 : 16)) & 255) != 0 ? 1 : 0;
           }
           int tot;
           int inc = block_inclusive_scan<int>(f, s.sh, &tot);
@@ -767,8 +782,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
           if (gkeep[jj]) {
             const int2 gg = Gh[GA[jj]];
             const int g = gg.y & 255;
-            const int cx = a.cc[(size_t)gg.x * d + D];
-            const int pt = chain_cut(a.lvl_pos[g], gg.y >> 8, pD, remc, gtD, cx >= c0 && cx <= c1);
+            const int gc = GC[GA[jj]];
+            const int cx = gc & 255;
+            const int pt = ((gc >> ((cx >= c0 && cx <= c1) ? 8 : 16)) & 255) - 1;
             const int o = atomicAdd(&s.gwrite, 1);
             if (o < s.gcount) a.out_ghosts[s.goff + o] = make_int2(gg.x, g | (pt << 8));
           }
