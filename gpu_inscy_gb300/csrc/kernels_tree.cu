@@ -37,9 +37,10 @@
 //                             child nodes (phantoms included) together with the
 //                             s-connection of the same cell, which decides which
 //                             ghosts survive.
-// All of this is integer work: filters are block-wide stable compactions and
-// the merge re-sort is a stable counting-sort per dim (warp match + block
-// scan).
+// All of this is integer work: filters are block-wide stable compactions; a
+// merged run is a stable partition by the cell on D (one counting pass: warp
+// match + block scan) and a merge of the cells' already ordered points; the
+// chain decisions test the nearest kept points in the sorted key order.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -561,11 +562,11 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_tree_level(TreeAr
       }
       __syncthreads();
       // 7. ghosts of the pruned tree.  A detached chain's fate mostly follows
-      //    from the points' nodes (range searches on the sorted point keys);
-      //    only a chain whose sibling node holds no point at all needs "does
-      //    a deeper chain pass this node", a range search on the chains' own
-      //    keys, so the region's chains are sorted by leaf key only when
-      //    some chain needs that.
+      //    from the points' nodes (its place among the sorted point keys and
+      //    the nearest kept points there); only a chain whose sibling node
+      //    holds no point at all needs "does a deeper chain pass this node",
+      //    a range search on the chains' own keys, so the region's chains are
+      //    sorted by leaf key only when some chain needs that.
       int ngp = 0;
       if (ng > 0) {
         for (int c = 0; c < ng; c += blockDim.x) {
