@@ -290,3 +290,15 @@ def test_row_kernel_tuner_keeps_the_lists(engine, monkeypatch):
     monkeypatch.setenv("INSCY_ROWS_TUNE", "0")
     got0, _ = gpu_run(X, **p)
     assert_same(got, (got0[0], got0[1]), "tuned vs default launch shape")
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_many_cells_long_merges_match_oracle(engine, seed):
+    """14 cells: runs of all 14 cells (eps above the cell width: the level
+    kernel's radix passes) and runs of a few cells (its partition + merge)."""
+    rng = np.random.default_rng(9100 + seed)
+    X = np.clip(rng.normal(0.5, 0.18, (3000, 5)), 0, 1).astype(np.float32)
+    p = dict(neighborhood_size=[0.09, 0.04][seed % 2], F=0.5, num_obj=2, min_size=6, r=1.0, number_of_cells=14,
+             rectangular=bool(seed // 2), entropy_order=[0, 1, -1, 0][seed])
+    got, _ = gpu_run(X, **p)
+    assert_same(got, orc.run(X, **p), "14 cells, seed %d" % seed)

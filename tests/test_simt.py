@@ -80,6 +80,25 @@ def test_family_cases_entropy_order(driver):
                     "family %d (entropy_order %d)" % (i, p["entropy_order"]))
 
 
+def many_cell_cases():
+    """14 cells: with eps above the cell width every point is s-connected on every
+    dim and a run merges all 14 cells (the level kernel's radix passes); with a
+    smaller eps runs merge a few cells (its partition + merge)."""
+    cases = []
+    for seed in range(4):
+        rng = np.random.default_rng(9100 + seed)
+        X = np.clip(rng.normal(0.5, 0.18, (600, 4)), 0, 1).astype(np.float32)
+        p = dict(neighborhood_size=[0.09, 0.04][seed % 2], F=0.5, num_obj=2, min_size=6, r=1.0, number_of_cells=14,
+                 rectangular=bool(seed // 2), entropy_order=[0, 1, -1, 0][seed])
+        cases.append((seed, X, p))
+    return cases
+
+
+def test_many_cells_long_merges(driver):
+    for seed, X, p in many_cell_cases():
+        assert_same(simt_run(driver, X, p, seed % 2 == 1, "cells%d" % seed), orc.run(X, **p), "14 cells, seed %d" % seed)
+
+
 def test_wide_rows(driver):
     # d = 20: the density pass on 32-slot point rows; d = 36: the general
     # density kernel and 128-bit leaf keys
