@@ -761,6 +761,8 @@ class Engine {
   std::vector<uint64_t> tbits_;               // region bitmap scratch
   std::vector<LoopVec> vbuf_;                  // one clustering vector per recursion depth
   std::vector<char> alive_;                    // join: clusters of the loop still alive
+  std::vector<int> sdesc_, hsel_;              // join: alive clusters by size; superset entries tested
+  std::vector<long long> spre_;                // join: prefix sums of those sizes
   std::vector<Walk> walk_, pieces_, split_;   // point ranges of the commit's loops
   std::unique_ptr<HostPool> hpool_;
   double t_prune_ = 0, t_cluster_ = 0, t_join_ = 0;
@@ -2105,10 +2107,36 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     // host pool when there are many.
     walk_.clear();
     long long total = 0;
+    // The same test from this loop's side: for a superset entry H, scan the
+    // members of every alive cluster here small enough for H's largest
+    // cluster to drop it.  Its cost (costB) is known from the clusters'
+    // sizes; the cheaper side runs (both drop exactly the same clusters).
+    sdesc_.clear();
+    for (int l = 1; l <= nl; ++l)
+      if (alive[l]) sdesc_.push_back(l);
+    std::sort(sdesc_.begin(), sdesc_.end(), [&](int x, int y) { return st.size[x] < st.size[y]; });
+    spre_.assign(sdesc_.size() + 1, 0);
+    for (size_t t = 0; t < sdesc_.size(); ++t) spre_[t + 1] = spre_[t] + st.size[sdesc_[t]];
+    // alive clusters (ascending size) with size * r < hmax: a prefix of sdesc_
+    auto below = [&](int hmax) {
+      size_t lo = 0, hi = sdesc_.size();
+      while (lo < hi) {
+        const size_t mid = (lo + hi) / 2;
+        if ((float)st.size[sdesc_[mid]] * hp_.r < (float)hmax)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      return lo;
+    };
+    long long costB = 0;
+    hsel_.clear();
     for (int i : superset_candidates(smask)) {
       Entry& H = *ents_[i];
       rc_[4]++;
       if (!((float)minsz * hp_.r < (float)H.maxsz)) continue;
+      hsel_.push_back(i);
+      costB += spre_[below(H.maxsz)];
       refresh_order(H);
       for (int t = (int)H.by_size.size() - 1; t >= 0; --t) {
         const int l = H.by_size[t];
@@ -2121,11 +2149,33 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         total += m;
       }
     }
-    rc_[5] += total;
     bool hit = false;
     const int* ssz = st.size.data();
     const float r = hp_.r;
-    if (total < kParallelWalk || hpool_->workers() == 0) {
+    if (costB < total && costB < kParallelWalk) {
+      rc_[5] += costB;
+      for (int i : hsel_) {
+        const Entry& H = *ents_[i];
+        const size_t nb = below(H.maxsz);
+        for (size_t t = 0; t < nb; ++t) {
+          const int l = sdesc_[t];
+          if (!alive[l]) continue;
+          const float lsz = (float)ssz[l] * r;
+          const HSub& hs = *st.ref[l].hs;
+          const int cp = st.ref[l].comp;
+          const int* mem = hs.members.data();
+          for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+            const int h = H.lab[mem[k]];
+            if (h >= 0 && lsz < (float)H.size[h]) {
+              alive[l] = 0;
+              hit = true;
+              break;
+            }
+          }
+        }
+      }
+    } else if (total < kParallelWalk || hpool_->workers() == 0) {
+      rc_[5] += total;
       // one thread: raise the size bar as clusters drop
       for (const Walk& w : walk_) {
         if (!((float)minsz * r < w.hsz)) continue;
@@ -2138,6 +2188,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         }
       }
     } else {
+      rc_[5] += total;
       pieces_.assign(walk_.begin(), walk_.end());
       split_pieces(total);
       std::atomic<bool> any{false};
