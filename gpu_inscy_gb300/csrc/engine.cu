@@ -2174,6 +2174,32 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
           }
         }
       }
+    } else if (costB < total && hpool_->workers() > 0) {
+      // the loop's side on the host pool: one task per alive cluster (largest
+      // first), which alone writes its own flag
+      rc_[5] += costB;
+      std::atomic<bool> any{false};
+      const int nsd = (int)sdesc_.size();
+      hpool_->run(nsd, [&](int t) {
+        const int l = sdesc_[nsd - 1 - t];
+        const float lsz = (float)ssz[l] * r;
+        const HSub& hs = *st.ref[l].hs;
+        const int cp = st.ref[l].comp;
+        const int* mem = hs.members.data();
+        for (int i : hsel_) {
+          const Entry& H = *ents_[i];
+          if (!(lsz < (float)H.maxsz)) continue;
+          for (long long k = hs.moff[cp]; k < hs.moff[cp + 1]; ++k) {
+            const int h = H.lab[mem[k]];
+            if (h >= 0 && lsz < (float)H.size[h]) {
+              alive[l] = 0;
+              any.store(true, std::memory_order_relaxed);
+              return;
+            }
+          }
+        }
+      });
+      hit = any.load();
     } else if (total < kParallelWalk || hpool_->workers() == 0) {
       rc_[5] += total;
       // one thread: raise the size bar as clusters drop
