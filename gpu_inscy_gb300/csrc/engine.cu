@@ -1942,17 +1942,23 @@ bool Engine::prune_redundancy(const Phase& ph, const HCall& c, uint64_t smask) {
   int max_min = 0;
   bool result = true;
   // An entry's minimum (its smallest cluster touching the region) is at most
-  // its largest cluster, so once max_min reaches an entry's largest cluster
-  // the entry cannot raise it; visiting the entries by largest cluster,
-  // largest first, the scan stops at the first such entry.  The answer
-  // depends only on the maximum over the entries, not on their order.
+  // its largest cluster, so an entry whose largest cluster is at or below
+  // max_min cannot raise it and is skipped.  The answer depends only on the
+  // maximum over the entries, not on their order: the entry with the largest
+  // cluster goes first (it tends to set a high max_min at once), the others
+  // in the order found.
   std::vector<int>& order = prune_order_;
   const std::vector<int>& sup = superset_candidates(smask);
   order.assign(sup.begin(), sup.end());
-  std::sort(order.begin(), order.end(), [&](int x, int y) { return ents_[x]->maxsz > ents_[y]->maxsz; });
+  if (order.size() > 1) {
+    size_t top = 0;
+    for (size_t t = 1; t < order.size(); ++t)
+      if (ents_[order[t]]->maxsz > ents_[order[top]]->maxsz) top = t;
+    std::swap(order[0], order[top]);
+  }
   for (int i : order) {
     Entry& E = *ents_[i];
-    if (E.maxsz <= max_min) break;
+    if (E.maxsz <= max_min) continue;
     int mn = -1;
     if (!use_bits) {
       // the entry matters only if its minimum ends above max_min, so the scan
