@@ -583,6 +583,8 @@ static bool walk_test(const Walk& w, const LoopVec& V, const int* size, float r,
 
 // joins whose redundancy test covers fewer points run it on one thread
 constexpr long long kParallelWalk = 32768;
+// device-to-host reads of at least this many bytes skip the pinned staging
+constexpr size_t kDirectD2H = 1u << 20;
 
 struct HostParams {
   float eps, F, r;
@@ -697,13 +699,23 @@ class Engine {
     CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
     return ms;
   }
+  // Small reads go through a pinned staging buffer; large ones (the levels'
+  // points, component members, borders and orders for the commit) are copied
+  // straight into their destination: on a host whose memory the GPU reaches
+  // coherently this skips a host copy of every byte (measured on the GB300
+  // host: the expansion of a 25,000 x 15 run 171 -> 160 ms).
   void d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     if (!bytes) return;
     auto t0 = std::chrono::steady_clock::now();
-    void* st = pinned_.get(bytes);
-    CK(cudaMemcpyAsync(st, src, bytes, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    std::memcpy(dst, st, bytes);
+    if (bytes >= kDirectD2H) {
+      CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    } else {
+      void* st = pinned_.get(bytes);
+      CK(cudaMemcpyAsync(st, src, bytes, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      std::memcpy(dst, st, bytes);
+    }
     stats_.d2h_bytes += (long long)bytes;
     stats_.ms_d2h += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
