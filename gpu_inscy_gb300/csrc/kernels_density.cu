@@ -921,6 +921,12 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
   const int2* acc = nullptr;  // the item's list entries
   int c = 0, j = 0;
   float sum = 0.f;
+  // phi is only compared with the weak, dense and keep thresholds
+  // (k_density_flags; keep <= weak), and the sum never decreases (every term
+  // 1 - sq >= 0, each rounding monotone): once it reaches the larger of the
+  // weak and the subspace's dense threshold every flag is decided, and the
+  // partial sum is stored
+  float stop = 0.f;
   bool live = false;  // this lane holds an item whose sum is still to be stored
   // hand the next items of the queue to the lanes in `need`, in lane order
   auto hand_out = [&](unsigned need) {
@@ -959,22 +965,29 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
       acc = a.ent + lo;
       j = 0;
       sum = 0.f;
+      if (live) {
+        const float td = a.thr_dense[a.subs[find_sub(a.subs, a.nsubs, item)].nsub];
+        stop = td > a.thr_weak ? td : a.thr_weak;
+      }
     }
   };
   new_batch();
   hand_out(0xffffffffu);
   for (;;) {
     if (!__any_sync(0xffffffffu, live)) break;
-    // steps every busy lane can take: the shortest remaining list
+    // steps every busy lane can take: the shortest remaining list, at most
+    // 128 so that lanes whose sums stop early are refilled soon
     int steps = live ? c - j : INT_MAX;
     for (int o = 16; o > 0; o >>= 1) steps = min(steps, __shfl_xor_sync(0xffffffffu, steps, o));
+    steps = min(steps, 128);
     if (live) {
       // the terms do not depend on the sum: four at a time are loaded and
       // computed side by side, then added in order (the sum's chain alone is
       // sequential)
       const int2* ap = acc + j;
       int t = 0;
-      for (; t + 4 <= steps; t += 4) {
+      bool hit = sum >= stop;
+      for (; !hit && t + 4 <= steps; t += 4) {
         const float a0 = __int_as_float(ap[t].y), a1 = __int_as_float(ap[t + 1].y);
         const float a2 = __int_as_float(ap[t + 2].y), a3 = __int_as_float(ap[t + 3].y);
         const float d0 = __fdiv_rn(__fsqrt_rn(a0), a.eps), d1 = __fdiv_rn(__fsqrt_rn(a1), a.eps);
@@ -983,12 +996,14 @@ __global__ void __launch_bounds__(256, kPhiBlocksPerSM) k_density_phi(DensityArg
         sum = phi_step_exact(sum, __fmul_rn(d1, d1));
         sum = phi_step_exact(sum, __fmul_rn(d2, d2));
         sum = phi_step_exact(sum, __fmul_rn(d3, d3));
+        hit = sum >= stop;
       }
-      for (; t < steps; ++t) {
+      for (; !hit && t < steps; ++t) {
         const float dd = __fdiv_rn(__fsqrt_rn(__int_as_float(ap[t].y)), a.eps);
         sum = phi_step_exact(sum, __fmul_rn(dd, dd));
+        hit = sum >= stop;
       }
-      j += steps;
+      j = hit ? c : j + steps;
     }
     const bool done = live && j >= c;
     if (done) {
