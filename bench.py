@@ -188,7 +188,7 @@ def batched_block(_lib):
     # autotune the lane count on the first 24 datasets
     sub = Xs[:24]
     tried = {}
-    for lanes in (2, 4, 8):
+    for lanes in (2, 4, 8, 12, 16):
         _lib.run_batch(sub, params, _lib.MODE_BATCHED, lanes=lanes)  # warm the lanes' engines
         t0 = time.perf_counter()
         _lib.run_batch(sub, params, _lib.MODE_BATCHED, lanes=lanes)
