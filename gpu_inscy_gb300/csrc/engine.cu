@@ -449,12 +449,6 @@ struct LoopVec {
 
 // The clusters numbered in one dim loop (the reference's shared clustering
 // vector): label l -> component, and its size.
-struct LoopState {
-  std::vector<LabelRef> ref{LabelRef{nullptr, -1}};
-  std::vector<int> size{0};
-  int nlabels = 0;
-};
-
 // Host threads for the data-parallel loops of the commit.  run(tasks, fn)
 // calls fn(i) for every i in [0, tasks) on the workers and the calling
 // thread and returns when all are done.  Only as many workers as there are
@@ -550,6 +544,17 @@ struct Walk {
   const int* lab;
   int l;
   float hsz;
+};
+
+struct LoopState {
+  std::vector<LabelRef> ref{LabelRef{nullptr, -1}};
+  std::vector<int> size{0};
+  int nlabels = 0;
+  // loop-vector writes of the members of min_size clusters (their first
+  // member is written at once), made only when join's redundancy test reads
+  // the loop vector (its superset side)
+  std::vector<Walk> pend;
+  long long pend_work = 0;
 };
 
 // Drop every live cluster c of the loop with a point in w and
@@ -746,6 +751,7 @@ class Engine {
   const std::vector<int>& superset_candidates(uint64_t smask);
   void cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState& st);
   void join(LoopVec& V, LoopState& st, uint64_t smask);
+  void flush_pending(LoopVec& V, LoopState& st);
   void split_pieces(long long work);
 
   int device_ = 0;
@@ -2036,7 +2042,6 @@ void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState
   // changes another component's first member: all labels can be decided
   // before the writes.
   const int first = st.nlabels + 1;
-  long long work = 0;
   // three dependent random reads per component (its member range, its first
   // member, that member's label): each is prefetched a few components ahead
   // of its use, the next read in the chain once the previous one has landed
@@ -2059,7 +2064,6 @@ void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState
     rc_[9] += hs.boff[comp + 1] - hs.boff[comp];
     st.ref.push_back(LabelRef{&hs, comp});
     st.size.push_back((int)(m1 - m0));
-    if (m1 - m0 >= hp_.min_size) work += m1 - m0;
   }
   // The loop vector is read in two places only: the check above (a
   // component's first member) and join's redundancy test, which looks at
@@ -2067,27 +2071,40 @@ void Engine::cluster_into(const Phase& ph, const HCall& c, LoopVec& V, LoopState
   // those clusters get every member labelled and the others their first
   // member; the -2 marks of border points reach the result entry from the
   // component lists in join and are never read from the loop vector.
+  // The other members of the clusters that join may test are written only if
+  // join reads the loop vector (flush_pending): its test from the loop's side
+  // does not.
   uint64_t* gv = V.gv.data();
   const uint64_t cur = V.cur;
-  pieces_.clear();
   for (int label = first; label <= st.nlabels; ++label) {
     const int comp = st.ref[label].comp;
     const long long m0 = hs.moff[comp], m = hs.moff[comp + 1] - m0;
-    if (m >= hp_.min_size && m > 1)
-      pieces_.push_back(Walk{hs.members.data() + m0, 0, m, nullptr, label, 0.f});
-    else
-      gv[hs.members[m0]] = cur | (uint32_t)label;
+    gv[hs.members[m0]] = cur | (uint32_t)label;
+    if (m >= hp_.min_size && m > 1) {
+      st.pend.push_back(Walk{hs.members.data() + m0, 1, m, nullptr, label, 0.f});
+      st.pend_work += m - 1;
+    }
   }
+}
+
+// the loop-vector writes cluster_into left pending
+void Engine::flush_pending(LoopVec& V, LoopState& st) {
+  if (st.pend.empty()) return;
+  uint64_t* gv = V.gv.data();
+  const uint64_t cur = V.cur;
   auto write = [&](const Walk& w) {
     const uint64_t v = cur | (uint32_t)w.l;
     for (long long k = w.k0; k < w.k1; ++k) __atomic_store_n(&gv[w.mem[k]], v, __ATOMIC_RELAXED);
   };
-  if (work < kParallelWalk || hpool_->workers() == 0) {
-    for (const Walk& w : pieces_) write(w);
-    return;
+  if (st.pend_work < kParallelWalk || hpool_->workers() == 0) {
+    for (const Walk& w : st.pend) write(w);
+  } else {
+    pieces_.assign(st.pend.begin(), st.pend.end());
+    split_pieces(st.pend_work);
+    hpool_->run((int)split_.size(), [&](int i) { write(split_[i]); });
   }
-  split_pieces(work);
-  hpool_->run((int)split_.size(), [&](int i) { write(split_[i]); });
+  st.pend.clear();
+  st.pend_work = 0;
 }
 
 // pieces_ cut into parts of about work / (4 * threads) entries (split_)
@@ -2219,6 +2236,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       });
       hit = any.load();
     } else if (total < kParallelWalk || hpool_->workers() == 0) {
+      flush_pending(V, st);
       rc_[5] += total;
       // one thread: raise the size bar as clusters drop
       for (const Walk& w : walk_) {
@@ -2232,6 +2250,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
         }
       }
     } else {
+      flush_pending(V, st);
       rc_[5] += total;
       pieces_.assign(walk_.begin(), walk_.end());
       split_pieces(total);
@@ -2248,6 +2267,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
       if (minsz == INT32_MAX) return;
     }
   } else {
+    flush_pending(V, st);
     for (int i : superset_candidates(smask)) {
       Entry& H = *ents_[i];
       rc_[4]++;
