@@ -2187,7 +2187,9 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
     bool hit = false;
     const int* ssz = st.size.data();
     const float r = hp_.r;
-    if (costB < total && costB < kParallelWalk) {
+    // the superset side also pays for the loop-vector writes left pending
+    const long long costA = total + st.pend_work;
+    if (costB < costA && costB < kParallelWalk) {
       rc_[5] += costB;
       for (int i : hsel_) {
         const Entry& H = *ents_[i];
@@ -2209,7 +2211,7 @@ void Engine::join(LoopVec& V, LoopState& st, uint64_t smask) {
           }
         }
       }
-    } else if (costB < total && hpool_->workers() > 0) {
+    } else if (costB < costA && hpool_->workers() > 0) {
       // the loop's side on the host pool: one task per alive cluster (largest
       // first), which alone writes its own flag
       rc_[5] += costB;
