@@ -251,16 +251,40 @@ struct HCall {
   std::vector<HRegion> regions;  // ordered by (dim, cell run)
 };
 
+// ints read back from the device: resize() gives fresh storage without
+// filling it (the copy fills it)
+struct IntBuf {
+  std::unique_ptr<int[]> p;
+  size_t n = 0;
+  void resize(size_t m) {
+    p.reset(new int[m > 0 ? m : 1]);
+    n = m;
+  }
+  int* data() { return p.get(); }
+  const int* data() const { return p.get(); }
+  size_t size() const { return n; }
+};
+
+// a read-only range of such a buffer
+struct IntView {
+  const int* p = nullptr;
+  size_t n = 0;
+  const int* data() const { return p; }
+  const int& operator[](size_t i) const { return p[i]; }
+  size_t size() const { return n; }
+};
+
 struct HLevel {
-  std::vector<int> pts;
-  std::vector<int> order;
+  IntBuf pts;
+  IntBuf order;
 };
 
 struct HSub {  // components of one clustered subspace
   std::vector<long long> moff;
-  std::vector<int> members;
+  IntView members;  // ranges of the level's member and border read-backs,
   std::vector<long long> boff;
-  std::vector<int> borders;
+  IntView borders;
+  std::shared_ptr<const IntBuf> keep_m, keep_b;  // which these keep alive
 };
 
 // Where the points of a label come from: component `comp` of a clustered
@@ -1697,9 +1721,11 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
         hmoff[ncomp] = hm[0];
         d2h(hboff.data(), boff, sizeof(long long) * ncomp, s);
         hboff[ncomp] = hb;
-        std::vector<int> hmem(hm[0]), hbor(hb);
-        d2h(hmem.data(), members, sizeof(int) * hm[0], s);
-        d2h(hbor.data(), borders, sizeof(int) * hb, s);
+        auto hmem = std::make_shared<IntBuf>(), hbor = std::make_shared<IntBuf>();
+        hmem->resize(hm[0]);
+        hbor->resize(hb);
+        d2h(hmem->data(), members, sizeof(int) * hm[0], s);
+        d2h(hbor->data(), borders, sizeof(int) * hb, s);
         std::vector<int> hocnt(ncall.size());
         long long* order_off = lv.get<long long>(ncall.size() + 1);
         long long* dot = lv.get<long long>(1);
@@ -1726,8 +1752,10 @@ void Engine::run(const float* X, bool on_device, long long n, int d, const HostP
             hs.moff[c - c0] = hmoff[c] - hmoff[c0];
             hs.boff[c - c0] = hboff[c] - hboff[c0];
           }
-          hs.members.assign(hmem.begin() + hmoff[c0], hmem.begin() + hmoff[c1]);
-          hs.borders.assign(hbor.begin() + hboff[c0], hbor.begin() + hboff[c1]);
+          hs.members = IntView{hmem->data() + hmoff[c0], (size_t)(hmoff[c1] - hmoff[c0])};
+          hs.borders = IntView{hbor->data() + hboff[c0], (size_t)(hboff[c1] - hboff[c0])};
+          hs.keep_m = hmem;
+          hs.keep_b = hbor;
           Phase& sp = phases_[phase < 0 ? phase_of_[subs[i].dim] : phase];
           csub_of[i] = (int)sp.subs.size();
           sp.subs.push_back(std::move(hs));
