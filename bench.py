@@ -24,9 +24,14 @@ clustered per second (n / run time) and ms per run.
              cores.
 
 batched -- the 64-dataset batch workload: plain runs one after another vs the
-             batched form (concurrent lanes) with FIFO and with the learned
-             schedule (cost model trained on the committed cost records).
-large_d -- one run of the 100,000 x 25 workload (e2e, host buffers).
+             batched form (concurrent lanes; the lane count timed among 2, 4
+             and 8 on 24 of the datasets) with FIFO and with the learned
+             schedule (cost model trained on the committed cost records),
+             three alternating runs of each, the best counting; labels against
+             the plain runs and the oracle fixtures of 8 datasets.
+large_d -- the 100,000 x 25 workload, one warm-up run then one timed (e2e,
+             host buffers), labels against its oracle fixture.
+autotune -- the row kernel's launch shape the engine's tuner chose.
 real_shapes -- e2e ms per run on stand-ins with the sizes of the reference's
              real-data runs and its real-data parameters, next to the wall
              times the reference publishes for GPU-INSCY on the real datasets
