@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256) k_uf_dominant(ClusterArgs a, const int* _
 // the larger keep index (the other one's warp skips it; the neighbour relation
 // is symmetric), an edge to a dominant point always; edges between dominant
 // points join one component already.  The point's own root is found once per
-// 32 neighbours.
+// 64 neighbours.
 __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const uint8_t* __restrict__ dom) {
   const long long kk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (kk >= a.nkeep) return;
@@ -207,25 +207,42 @@ __global__ void __launch_bounds__(256) k_uf_union(ClusterArgs a, const uint8_t* 
   const unsigned lane = lane_id();
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
-  for (int j0 = 0; j0 < len; j0 += 32) {
-    const int j = j0 + (int)lane;
-    int kq = -1;
-    if (j < len) {
-      int q = a.ent[b + j].x;
-      if (GUARD_OK(a.guard, q >= 0 && q < a.n, 61, q) && bit_of(dn, q)) {
-        long long k2 = keep_index(a, si, q);
-        if (GUARD_OK(a.guard, k2 >= a.kstart[si] && k2 < a.kstart[si + 1], 62, k2))
-          kq = (k2 < kk || dom[k2]) ? (int)k2 : -1;  // a larger non-dominant neighbour takes the edge
+  // two chunks of 32 entries per step: their loads and finds are independent
+  // chains, issued together (the walk is bound by their latency)
+  constexpr int kUnionChunks = 2;
+  for (int j0 = 0; j0 < len; j0 += kUnionChunks * 32) {
+    int qv[kUnionChunks], kq[kUnionChunks];
+#pragma unroll
+    for (int u = 0; u < kUnionChunks; ++u) {
+      const int j = j0 + u * 32 + (int)lane;
+      qv[u] = j < len ? a.ent[b + j].x : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kUnionChunks; ++u) {
+      kq[u] = -1;
+      if (j0 + u * 32 + (int)lane < len) {
+        const int q = qv[u];
+        if (GUARD_OK(a.guard, q >= 0 && q < a.n, 61, q) && bit_of(dn, q)) {
+          long long k2 = keep_index(a, si, q);
+          if (GUARD_OK(a.guard, k2 >= a.kstart[si] && k2 < a.kstart[si + 1], 62, k2))
+            kq[u] = (k2 < kk || dom[k2]) ? (int)k2 : -1;  // a larger non-dominant neighbour takes the edge
+        }
       }
     }
-    if (!__any_sync(0xffffffffu, kq >= 0)) continue;
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < kUnionChunks; ++u) any = any || kq[u] >= 0;
+    if (!__any_sync(0xffffffffu, any)) continue;
     int rk = 0;
     if (lane == 0) rk = uf_find(a.uf, (int)kk);
     rk = __shfl_sync(0xffffffffu, rk, 0);
-    if (kq >= 0) {
-      int rq = uf_find(a.uf, kq);
-      if (rq != rk) uf_unite(a.uf, rk, rq, a.err);
-    }
+    int rq[kUnionChunks];
+#pragma unroll
+    for (int u = 0; u < kUnionChunks; ++u) rq[u] = kq[u] >= 0 ? uf_find(a.uf, kq[u]) : rk;
+    // uf_unite takes stale roots: a failed hook finds the current ones
+#pragma unroll
+    for (int u = 0; u < kUnionChunks; ++u)
+      if (rq[u] != rk) uf_unite(a.uf, rk, rq[u], a.err);
   }
 }
 
@@ -367,27 +384,40 @@ __global__ void __launch_bounds__(256) k_borders(ClusterArgs a, const int* __res
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
   int* sl = slots + (long long)cslot_of[si] * a.n * 2;
-  for (int j = lane_id(); j < len; j += 32) {
-    int q = a.ent[b + j].x;
-    if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 65, q) || bit_of(dn, q)) continue;
-    int* s2 = sl + 2LL * q;
-    int v0 = ((volatile int*)s2)[0];
-    if (v0 == c) continue;
-    if (v0 == -1) {
-      int old = atomicCAS(&s2[0], -1, c);
-      if (old == -1 || old == c) continue;
+  // the list is read kBorderChunks x 32 entries at a time, all loads issued
+  // before the first is used (the walk is bound by their latency)
+  constexpr int kBorderChunks = 4;
+  for (int j0 = 0; j0 < len; j0 += kBorderChunks * 32) {
+    int qv[kBorderChunks];
+#pragma unroll
+    for (int u = 0; u < kBorderChunks; ++u) {
+      const int j = j0 + u * 32 + (int)lane_id();
+      qv[u] = j < len ? a.ent[b + j].x : 0;
     }
-    int v1 = ((volatile int*)s2)[1];
-    if (v1 == c) continue;
-    if (v1 == -1) {
-      int old = atomicCAS(&s2[1], -1, c);
-      if (old == -1 || old == c) continue;
+#pragma unroll
+    for (int u = 0; u < kBorderChunks; ++u) {
+      if (j0 + u * 32 + (int)lane_id() >= len) continue;
+      const int q = qv[u];
+      if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 65, q) || bit_of(dn, q)) continue;
+      int* s2 = sl + 2LL * q;
+      int v0 = ((volatile int*)s2)[0];
+      if (v0 == c) continue;
+      if (v0 == -1) {
+        int old = atomicCAS(&s2[0], -1, c);
+        if (old == -1 || old == c) continue;
+      }
+      int v1 = ((volatile int*)s2)[1];
+      if (v1 == c) continue;
+      if (v1 == -1) {
+        int old = atomicCAS(&s2[1], -1, c);
+        if (old == -1 || old == c) continue;
+      }
+      int o = atomicAdd(novf, 1);
+      if (o < ovf_cap)
+        ovf[o] = make_int2(c, q);
+      else
+        atomicExch(a.err, 4);
     }
-    int o = atomicAdd(novf, 1);
-    if (o < ovf_cap)
-      ovf[o] = make_int2(c, q);
-    else
-      atomicExch(a.err, 4);
   }
 }
 
