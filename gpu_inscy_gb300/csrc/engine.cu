@@ -2400,7 +2400,7 @@ class LanePool {
     inscy::t_pool_workers = std::max(0, std::min(7, hw / (2 * lanes_) - 1));
     inscy::t_single_pass_bytes = inscy::kSinglePassBytes / lanes_;
     cudaStream_t s = nullptr;
-    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    const cudaError_t serr = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     long long seen = 0;
     for (;;) {
       std::vector<BatchJob>* jobs;
@@ -2417,6 +2417,11 @@ class LanePool {
         const int i = next_.fetch_add(1);
         if (i >= (int)jobs->size()) break;
         BatchJob& j = (*jobs)[i];
+        if (serr != cudaSuccess) {  // the lane has no stream: its datasets fail
+          j.rc = INSCY_ERR_CUDA;
+          j.err = std::string("lane stream: ") + cudaGetErrorString(serr);
+          continue;
+        }
         j.rc = run_common(j.X, false, j.n, j.d, p, s, j.out);
         if (j.rc) j.err = g_err;
       }
@@ -2424,7 +2429,7 @@ class LanePool {
       if (--active_ == 0) done_.notify_all();
     }
     g_engine.reset();
-    cudaStreamDestroy(s);
+    if (serr == cudaSuccess) cudaStreamDestroy(s);
   }
   int device_, lanes_;
   bool stop_ = false;
