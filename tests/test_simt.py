@@ -99,6 +99,34 @@ def test_many_cells_long_merges(driver):
         assert_same(simt_run(driver, X, p, seed % 2 == 1, "cells%d" % seed), orc.run(X, **p), "14 cells, seed %d" % seed)
 
 
+def long_list_cases():
+    """Two tight clusters of 200 points and 100 noise points in [0, 1]^4, eps
+    0.12 / 0.15: every clustered point has ~200 neighbours, so the border walk
+    takes a full step of four 32-entry chunks and a partial one, and the union
+    walk (the cluster outside the sampled dominant component) several steps of
+    two chunks; the noise points near the clusters are border points.  A
+    skipped border chunk changes the labels of both cases; the union walk's
+    reads are checked against the guard pages here (a tight cluster stays
+    connected without a third of its edges), its edges by the full-size
+    fixtures on the GPU."""
+    cases = []
+    for seed, eps in ((1, 0.12), (2, 0.15)):
+        rng = np.random.default_rng(seed)
+        c1 = rng.normal([0.25, 0.3, 0.7, 0.5], 0.03, (200, 4))
+        c2 = rng.normal([0.75, 0.7, 0.3, 0.5], 0.03, (200, 4))
+        X = np.clip(np.vstack([c1, c2, rng.uniform(0, 1, (100, 4))]), 0, 1).astype(np.float32)
+        p = dict(neighborhood_size=eps, F=1.0, num_obj=4, min_size=20, r=1.0, number_of_cells=3)
+        cases.append((seed, X, p))
+    return cases
+
+
+def test_long_neighbour_lists(driver):
+    for seed, X, p in long_list_cases():
+        want = orc.run(X, **p)
+        assert any(len(set(lab.tolist()) - {-1, -2}) >= 2 and (lab == -2).any() for lab in want[1])
+        assert_same(simt_run(driver, X, p, seed % 2 == 0, "long%d" % seed), want, "long lists, seed %d" % seed)
+
+
 def test_wide_rows(driver):
     # d = 20: the density pass on 32-slot point rows; d = 36: the general
     # density kernel and 128-bit leaf keys
