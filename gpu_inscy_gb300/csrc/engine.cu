@@ -596,7 +596,7 @@ class Engine {
     d2h(&v, dev, sizeof(T), s);
     return v;
   }
-  void* scan_sums(long long n, cudaStream_t s, Scope& sc) {
+  void* scan_sums(long long n, cudaStream_t, Scope& sc) {
     long long nt = (n + 2047) / 2048 + 1;
     return sc.get<long long>((size_t)nt);
   }

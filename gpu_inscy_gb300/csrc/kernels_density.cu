@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(256, rows_blocks_per_sm(kS)) k_neighbours_rows
 #define INSCY_ROWS_TMA_BUFFERS16 3
 #endif
 __host__ __device__ constexpr int rows_tma_buffers(int kS) { return kS == 16 ? INSCY_ROWS_TMA_BUFFERS16 : 2; }
-__host__ __device__ constexpr int rows_tma_blocks(int kS) { return 3; }
+__host__ __device__ constexpr int rows_tma_blocks(int) { return 3; }
 __host__ __device__ constexpr int rows_tma_smem(int kS) { return 8 * rows_tma_buffers(kS) * 32 * kS * 4; }
 // an mbarrier wait gives up after this many polls (the copies of a chunk take
 // microseconds), reports guard code 36 and stops the warp
