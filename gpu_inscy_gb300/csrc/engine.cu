@@ -2465,8 +2465,8 @@ int inscy_run_device(const float* X_dev, int64_t n, int d, const inscy_params* p
 int inscy_run_batch_scheduled(const float* const* Xs, const int64_t* ns, const int* ds, int count,
                               const inscy_params* p, const int* order, int lanes, inscy_result** outs) {
   if (count < 0 || (count > 0 && (!Xs || !ns || !ds || !outs))) return fail(INSCY_ERR_ARG, "bad batch arguments");
+  for (int i = 0; i < count; ++i) outs[i] = nullptr;  // on every failure below they stay NULL
   if (lanes < 1 || lanes > 64) return fail(INSCY_ERR_ARG, "lanes must be in [1, 64]");
-  for (int i = 0; i < count; ++i) outs[i] = nullptr;
   if (count == 0) return INSCY_OK;
   std::vector<char> seen(count, 0);
   std::vector<BatchJob> jobs(count);
@@ -2522,7 +2522,7 @@ int inscy_result_count(const inscy_result* r) { return r ? (int)r->dims.size() :
 int64_t inscy_result_n(const inscy_result* r) { return r ? r->n : 0; }
 
 int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap) {
-  if (!r || i < 0 || i >= (int)r->dims.size()) return -1;
+  if (!r || i < 0 || i >= (int)r->dims.size() || (cap > 0 && !dims)) return -1;
   const auto& v = r->dims[i];
   for (int k = 0; k < (int)v.size() && k < cap; ++k) dims[k] = v[k];
   return (int)v.size();

@@ -110,7 +110,7 @@ int inscy_run_device(const float* X_dev, int64_t n, int d, const inscy_params* p
 
 /* Many independent datasets (the batched workload): outs[i] receives the
  * result of Xs[i] ([ns[i], ds[i]], host).  Same semantics as `count` calls of
- * inscy_run. */
+ * inscy_run; on failure every outs[i] is NULL. */
 int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, int count, const inscy_params* p,
                     int mode, inscy_result** outs);
 
@@ -121,7 +121,8 @@ int inscy_run_batch(const float* const* Xs, const int64_t* ns, const int* ds, in
  * dataset of `order` (a permutation of 0..count-1; NULL: 0, 1, ...), so the
  * order is the schedule (a cost model can put the longest datasets first).
  * outs[i] receives the result of Xs[i], identical to inscy_run's.  1 <= lanes
- * <= 64.  Calls are serialised within a process. */
+ * <= 64.  Calls are serialised within a process.  On failure every outs[i]
+ * is NULL (results of datasets that had finished are freed). */
 int inscy_run_batch_scheduled(const float* const* Xs, const int64_t* ns, const int* ds, int count,
                               const inscy_params* p, const int* order, int lanes, inscy_result** outs);
 
@@ -147,7 +148,8 @@ const char* inscy_mlp_last_error(void);
 /* Result access. */
 int inscy_result_count(const inscy_result* r);              /* number of clustered subspaces */
 int64_t inscy_result_n(const inscy_result* r);              /* number of points */
-int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap); /* returns |S|, writes min(|S|,cap) dims */
+int inscy_result_subspace(const inscy_result* r, int i, int* dims, int cap); /* returns |S|, writes min(|S|,cap) dims;
+                                                                          -1: bad index, or dims NULL with cap > 0 */
 int inscy_result_labels(const inscy_result* r, int i, int32_t* out);        /* copies n labels */
 const int32_t* inscy_result_labels_ptr(const inscy_result* r, int i);       /* n labels, valid until free; NULL on bad i */
 /* The whole result in a few calls (no counterpart in the reference, whose

@@ -76,7 +76,44 @@ def test_null_output_pointer(engine):
 def test_result_accessors_tolerate_null(engine):
     assert engine.inscy_result_count(None) == 0
     assert engine.inscy_result_n(None) == 0
+    assert engine.inscy_result_subspace(None, 0, None, 0) == -1
+    assert engine.inscy_result_labels(None, 0, None) == _lib.INSCY_ERR_ARG
+    assert engine.inscy_result_labels_ptr(None, 0) is None
+    assert engine.inscy_result_subspaces(None, None, 0, None) == -1
+    assert engine.inscy_result_label_blocks(None, None) == -1
+    assert engine.inscy_result_label_block(None, 0) is None
+    assert engine.inscy_result_label_slots(None, None) == _lib.INSCY_ERR_ARG
+    assert engine.inscy_result_stats(None, None) == _lib.INSCY_ERR_ARG
     engine.inscy_result_free(None)
+
+
+def _batch_args(Xs):
+    B = len(Xs)
+    vp = ctypes.c_void_p
+    return ((vp * B)(*[x.ctypes.data for x in Xs]), (ctypes.c_int64 * B)(*[x.shape[0] for x in Xs]),
+            (ctypes.c_int * B)(*[x.shape[1] for x in Xs]), (vp * B)(*([1] * B)))
+
+
+def test_batch_arguments_are_rejected(engine):
+    """The batch entries check their arguments before any CUDA call: lanes
+    outside [1, 64], an order that is no permutation, a negative count; every
+    output handle is left NULL."""
+    p = _lib.make_params(0.1, 1.0, 2, 4, 1.0, 4)
+    Xs = [np.random.default_rng(i).random((20, 3)).astype(np.float32) for i in range(2)]
+    ip = ctypes.POINTER(ctypes.c_int)
+    for order, lanes in ((None, 0), (None, 65), ((0, 0), 2), ((0, 2), 2), ((1, -1), 2)):
+        ptrs, ns, ds, outs = _batch_args(Xs)
+        ordp = None if order is None else ctypes.cast((ctypes.c_int * 2)(*order), ip)
+        rc = engine.inscy_run_batch_scheduled(ptrs, ns, ds, 2, ctypes.byref(p), ordp, lanes, outs)
+        assert rc == _lib.INSCY_ERR_ARG, (order, lanes)
+        assert engine.inscy_last_error().decode()
+        assert list(outs) == [None, None], (order, lanes)
+    ptrs, ns, ds, outs = _batch_args(Xs)
+    assert engine.inscy_run_batch_scheduled(ptrs, ns, ds, -1, ctypes.byref(p), None, 2, outs) == _lib.INSCY_ERR_ARG
+    assert engine.inscy_run_batch(ptrs, ns, ds, -1, ctypes.byref(p), _lib.MODE_PLAIN, outs) == _lib.INSCY_ERR_ARG
+    # no datasets: nothing to run, success
+    assert engine.inscy_run_batch(ptrs, ns, ds, 0, ctypes.byref(p), _lib.MODE_PLAIN, outs) == _lib.INSCY_OK
+    assert engine.inscy_run_batch_scheduled(ptrs, ns, ds, 0, ctypes.byref(p), None, 2, outs) == _lib.INSCY_OK
 
 
 def test_missing_library_fails_loudly(monkeypatch):
