@@ -35,7 +35,7 @@ static void pool_runs_every_task() {
 // ended and rethrows the first exception; the pool stays usable
 static void pool_rethrows_after_all_tasks() {
   inscy::HostPool pool(4);
-  for (int round = 0; round < 20; ++round) {
+  for (int rep = 0; rep < 20; ++rep) {
     const int tasks = 200;
     std::vector<std::atomic<int>> hits(tasks);
     for (auto& h : hits) h = 0;
