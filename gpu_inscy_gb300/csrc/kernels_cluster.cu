@@ -107,6 +107,11 @@ __global__ void k_uf_init(int* par, long long n) {
 // neighbours.  Every edge that is skipped joins two points that were both in
 // the dominant component at some time, and components only grow, so the final
 // partition is the connected components of the full neighbour relation.
+// That holds for any number of links in (1): INSCY_UF_LINKS = 0 (a build for
+// the host tests) leaves every edge but the sampled point's to (3).
+#ifndef INSCY_UF_LINKS
+#define INSCY_UF_LINKS 2
+#endif
 
 // (1) one thread per kept point
 __global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
@@ -119,7 +124,7 @@ __global__ void __launch_bounds__(256) k_uf_link2(ClusterArgs a) {
   const long long b = a.keep_loff[kk];
   const int len = a.keep_lcnt[kk];
   int linked = 0;
-  for (int j = 0; j < len && linked < 2; ++j) {
+  for (int j = 0; j < len && linked < INSCY_UF_LINKS; ++j) {
     int q = a.ent[b + j].x;
     if (!GUARD_OK(a.guard, q >= 0 && q < a.n, 63, q) || !bit_of(dn, q)) continue;
     long long kq = keep_index(a, si, q);

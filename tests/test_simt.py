@@ -107,8 +107,8 @@ def long_list_cases():
     two chunks; the noise points near the clusters are border points.  A
     skipped border chunk changes the labels of both cases; the union walk's
     reads are checked against the guard pages here (a tight cluster stays
-    connected without a third of its edges), its edges by the full-size
-    fixtures on the GPU."""
+    connected without a third of its edges), its edges by the bridge cases of
+    the build without the link step (below)."""
     cases = []
     for seed, eps in ((1, 0.12), (2, 0.15)):
         rng = np.random.default_rng(seed)
@@ -155,6 +155,49 @@ def driver_key64():
     import build_simt
     # also keeps the general density kernel (no point rows) for d <= 16
     return build_simt.build(defines=("INSCY_TREE_MIN_KEY_BYTES=8", "INSCY_DENSITY_ROWS=0"), tag="_key64")
+
+
+@pytest.fixture(scope="module")
+def driver_links0():
+    import build_simt
+    # no link step before the dominant-component sample: the union walk takes
+    # every edge (but the sampled point's), so its chunks all count
+    return build_simt.build(defines=("INSCY_UF_LINKS=0",), tag="_links0")
+
+
+def bridge_cases():
+    """A small blob (60 points, the lowest point ids) beside a large one (300
+    points) and 40 noise points in [0, 1]^3: in subspace {0, 1} the two blobs
+    are one cluster, joined by the few pairs that lie within eps across the
+    gap.  Without the link step such an edge is taken only from the large
+    blob's side (the larger keep index), where the small blob's points come
+    after the large blob's neighbours in the list (fine-cell order on dim 0):
+    a union walk that drops a list's entries after the first 64, or one chunk
+    in three, splits the cluster in each of these cases."""
+    cases = []
+    for seed, eps, gap in ((0, 0.045, 0.10), (0, 0.05, 0.11), (1, 0.05, 0.12), (3, 0.05, 0.12)):
+        rng = np.random.default_rng(seed)
+        small = np.column_stack([rng.normal(0.40 + gap, 0.01, 60), rng.normal(0.5, 0.03, 60),
+                                 rng.normal(0.5, 0.02, 60)])
+        large = np.column_stack([rng.normal(0.40, 0.015, 300), rng.normal(0.5, 0.03, 300),
+                                 rng.normal(0.5, 0.02, 300)])
+        X = np.clip(np.vstack([small, large, rng.uniform(0, 1, (40, 3))]), 0, 1).astype(np.float32)
+        p = dict(neighborhood_size=eps, F=1.0, num_obj=4, min_size=20, r=1.0, number_of_cells=3)
+        cases.append((seed, X, p))
+    return cases
+
+
+def test_union_walk_takes_every_edge(driver_links0):
+    cases = [(seed, X, p) for seed, X, p in long_list_cases()]
+    for _, X, p in bridge_cases():
+        subs, labs = orc.run(X, **p)
+        lab = labs[subs.index([0, 1])]
+        assert lab[0] >= 0 and set(lab[:60].tolist()) == {lab[0]} and lab[60 + int(np.argmax(lab[60:360] >= 0))] == lab[0]
+    cases += [(200 + i, X, p) for i, (_, X, p) in enumerate(bridge_cases())]
+    cases += [(100 + i, X, p) for i, X, p, _ in [c for c in family_cases() if c[2]["entropy_order"] == 0][:4]]
+    for seed, X, p in cases:
+        assert_same(simt_run(driver_links0, X, p, seed % 2 == 1, "links0_%d" % seed), orc.run(X, **p),
+                    "no link step, case %d" % seed)
 
 
 @pytest.fixture(scope="module")
